@@ -1,0 +1,156 @@
+"""Oracle (test infrastructure only): t-SURFF surface flux of
+``src/tsurff.cpp`` on the momentum grid.
+
+* surface points: the Gauss points of every knot span clipped to [-R, R] on
+  each tangential axis, faces x_a = +-R (``tsurff.cpp:112-137,148-176``);
+* trace: psi and (1/m) d_n psi at each point (``tsurff.cpp:220-243``);
+* Volkov integrals A' = -s E, B' = A, C' = |A|^2/2m + V0 by classical RK4 on
+  substeps of at most TimeStep/2 (``tsurff.cpp:395-428``);
+* flux per momentum (``FluxList``, ``tsurff.cpp:536-559``; the grid path
+  ``FluxGrid`` ``:478-534`` is the same sum factorised by axis);
+* trapezoid accumulation over samples (``AddFlux``, ``tsurff.cpp:439-469``).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .bspline import Space, find_span, ders_basis, gauss_legendre
+
+
+class OracleTSurff:
+    def __init__(self, space: Space, R: float, kgrid, mass: float, V0: float, sign: float,
+                 field, dt: float, nq: int = 0, inv_mass_at=None):
+        self.space = space
+        self.dim = space.dim
+        self.R = R
+        self.mass = mass
+        self.V0 = V0
+        self.sign = sign
+        self.field = field          # t -> E_a(t), length dim (0 on uncoupled axes)
+        self.dt = dt
+        nq = nq or space.axes[0].nq
+        gx, gw = gauss_legendre(nq)
+        self.nodes, self.weights = [], []
+        for d in range(3):
+            if d >= self.dim:
+                self.nodes.append(np.array([0.0]))
+                self.weights.append(np.array([1.0]))
+                continue
+            U = space.axes[d].knots
+            xs, ws = [], []
+            for j in range(len(U) - 1):
+                lo, hi = max(U[j], -R), min(U[j + 1], R)
+                if hi <= lo:
+                    continue
+                for k in range(nq):
+                    xs.append(0.5 * (lo + hi) + 0.5 * (hi - lo) * gx[k])
+                    ws.append(0.5 * (hi - lo) * gw[k])
+            self.nodes.append(np.array(xs))
+            self.weights.append(np.array(ws))
+        # surface points and trace rows
+        self.points = []    # (x[3], w, face, invMass)
+        rows_v, rows_n = [], []
+        for a in range(self.dim):
+            for s in range(2):
+                sigma = 1.0 if s else -1.0
+                b = 1 if a == 0 else 0
+                c = 1 if a == 2 else 2
+                for ib, xb in enumerate(self.nodes[b]):
+                    for ic, xc in enumerate(self.nodes[c]):
+                        x = [0.0, 0.0, 0.0]
+                        x[a] = sigma * R
+                        x[b] = xb
+                        x[c] = xc
+                        w = self.weights[b][ib] * self.weights[c][ic]
+                        im = 1.0 / mass if inv_mass_at is None else inv_mass_at(*x)
+                        v, n = self._trace_row(x, a, sigma)
+                        self.points.append((np.array(x), w, 2 * a + s, im))
+                        rows_v.append(v)
+                        rows_n.append(n * im)
+        self.Tv = np.array(rows_v)
+        self.Tn = np.array(rows_n)
+        self.A = np.zeros(3)
+        self.B = np.zeros(3)
+        self.C = 0.0
+        self.vt = 0.0
+        self.prev = None
+        self.prevT = 0.0
+
+    def _trace_row(self, x, a, sigma):
+        """Dense rows: value and normal derivative of every basis function."""
+        sp_ = self.space
+        vals, ders = [], []
+        for d in range(self.dim):
+            ax = sp_.axes[d]
+            s = find_span(ax.knots, ax.p, ax.n, x[d])
+            D = ders_basis(ax.knots, ax.p, s, x[d], 1)
+            v = np.zeros(ax.n)
+            dv = np.zeros(ax.n)
+            v[s - ax.p:s + 1] = D[0]
+            dv[s - ax.p:s + 1] = D[1]
+            vals.append(v)
+            ders.append(dv)
+        V = vals[-1]
+        N = ders[-1] if a == self.dim - 1 else vals[-1]
+        for d in reversed(range(self.dim - 1)):
+            V = np.kron(V, vals[d])
+            N = np.kron(N, ders[d] if a == d else vals[d])
+        return V, sigma * N
+
+    def advance_volkov(self, t):
+        h = t - self.vt
+        if h <= 0:
+            return
+        n = max(1, int(math.ceil(h / (0.5 * self.dt) - 1e-9)))
+        dt = h / n
+        s, m, V0 = self.sign, self.mass, self.V0
+
+        def f(tt, y):
+            E = self.field(tt)
+            dy = np.zeros(7)
+            for d in range(3):
+                dy[d] = -s * E[d] if d < self.dim else 0.0
+                dy[3 + d] = y[d]
+            dy[6] = (y[0] ** 2 + y[1] ** 2 + y[2] ** 2) / (2 * m) + V0
+            return dy
+        y = np.concatenate([self.A, self.B, [self.C]])
+        for i in range(n):
+            t0 = self.vt + i * dt
+            k1 = f(t0, y)
+            k2 = f(t0 + 0.5 * dt, y + 0.5 * dt * k1)
+            k3 = f(t0 + 0.5 * dt, y + 0.5 * dt * k2)
+            k4 = f(t0 + dt, y + dt * k3)
+            y = y + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        self.A, self.B, self.C = y[:3].copy(), y[3:6].copy(), float(y[6])
+        self.vt = t
+
+    def flux(self, psi, kgrid):
+        """Flux of psi at every momentum of the grid (list of per-axis arrays)."""
+        v = self.Tv @ psi
+        dn = self.Tn @ psi
+        ks = [np.asarray(kgrid[d]) if d < self.dim else np.array([0.0]) for d in range(3)]
+        K = np.stack(np.meshgrid(*ks, indexing="ij"), axis=-1).reshape(-1, 3)
+        out = np.zeros(len(K), dtype=np.complex128)
+        norm = (2 * math.pi) ** (-0.5 * self.dim)
+        for i, k in enumerate(K):
+            phi = self.C + np.sum(self.vt * k * k / (2 * self.mass) + k * self.B / self.mass)
+            kA = k + self.A
+            tot = 0j
+            for q, (x, w, face, im) in enumerate(self.points):
+                a = face // 2
+                sigma = 1.0 if face % 2 else -1.0
+                chi = w * np.exp(1j * (phi - kA @ x))
+                tot += chi * (-dn[q] - 1j * sigma * im * kA[a] * v[q])
+            out[i] = 0.5j * norm * tot
+        return out
+
+    def add_flux(self, t, psi, kgrid, amp):
+        self.advance_volkov(t)
+        cur = self.flux(psi, kgrid)
+        if self.prev is not None:
+            amp += 0.5 * (t - self.prevT) * (self.prev + cur)
+        self.prev = cur
+        self.prevT = t
+        return amp
