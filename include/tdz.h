@@ -1,0 +1,175 @@
+/*
+ * tdz.h - C ABI of the GB300 propagation library for TDSE-Z's hot path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes, no
+ * exceptions across the boundary. Vectors are device arrays of interleaved
+ * complex numbers (re, im) in the natural B-spline ordering, x fastest
+ * (index i + n_x (j + n_y k)); TDZ_FP32 means complex float (8 bytes per
+ * coefficient), TDZ_FP64 complex double (16 bytes). Device buffers passed in
+ * are owned by the caller; handles own their internal work buffers, which are
+ * allocated when the handle is created. Streams are cudaStream_t passed as
+ * void* (NULL = the legacy default stream).
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths are relative to the TDSE-Z source tree).
+ */
+#ifndef TDZ_H
+#define TDZ_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int tdz_status;
+#define TDZ_OK 0
+#define TDZ_ERR_ARG 1            /* invalid argument */
+#define TDZ_ERR_CUDA 2           /* CUDA runtime error */
+#define TDZ_ERR_NOT_CONVERGED 3  /* Krylov solve hit its iteration limit */
+#define TDZ_ERR_STATE 4          /* object not set up for this call */
+#define TDZ_ERR_UNSUPPORTED 5    /* configuration not supported */
+#define TDZ_ERR_BREAKDOWN 6      /* Krylov breakdown / non-finite residual */
+#define TDZ_ERR_INTERNAL 7
+
+#define TDZ_FP32 0
+#define TDZ_FP64 1
+
+/* operators selectable in tdz_operator_apply */
+#define TDZ_MASS 0        /* M  = int B_i B_j                                  */
+#define TDZ_HAMILTONIAN 1 /* H  = K[1/m] + s V (+ CAP if present)             */
+#define TDZ_DIPOLE_X 2    /* D_x = int x B_i B_j                               */
+#define TDZ_DIPOLE_Y 3
+#define TDZ_DIPOLE_Z 4
+#define TDZ_STAGE 5       /* A = alpha M + g (H + sum_a c_a D_a), see set_stage */
+
+typedef struct tdz_space tdz_space;
+typedef struct tdz_op tdz_op;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *tdz_last_error(void);
+
+/* Library version string. */
+const char *tdz_version(void);
+
+/* ---------------------------------------------------------------- space
+ * Tensor B-spline space: per axis (x first) a clamped knot vector of
+ * nknots[d] values and degree[d]; nquad Gauss-Legendre points per element
+ * and axis. Replaces the IGA set-up of src/core.cpp:1787-2046
+ * (IGASetQuadrature, IGAAxisSetKnots / IGAAxisInitUniform, IGASetUp).
+ */
+tdz_status tdz_space_create(int dim, const int *degree, const int *nknots, const double *const *knots,
+                            int nquad, tdz_space **out);
+/* n basis functions, nel non-empty knot spans and the degree of an axis. */
+tdz_status tdz_space_axis(const tdz_space *s, int axis, int *n, int *nel, int *degree);
+/* Total number of coefficients (prod_d n_d). */
+tdz_status tdz_space_ndof(const tdz_space *s, long long *ndof);
+/* Quadrature points and weights (times the element Jacobian) of one axis,
+ * nel*nquad values each, element-major (PetIGA IGABasis point/weight*detJac). */
+tdz_status tdz_space_quadrature(const tdz_space *s, int axis, double *x, double *w);
+void tdz_space_destroy(tdz_space *s);
+
+/* -------------------------------------------------------------- physics
+ * Separable carrier description. The potential and the mass are given as
+ * values at the 1D quadrature points, so that every operator is a sum of
+ * Kronecker products of 1D banded matrices:
+ *   V(r) = sum_d V_d(x_d)                 (pot_q[d], NULL = no term)
+ *   1/m  = inv_mass (mass_axis < 0) or 1/m(x_a) on axis a = mass_axis
+ *   CAP  = -i cap_inv_mass sum_d W_d(x_d) (cap_q[d], NULL = no layer)
+ * The carrier sign s = -charge multiplies V and the field terms
+ * (include/tdsez_parser.hpp:86-105,190-194).
+ */
+typedef struct tdz_physics {
+    double charge;              /* q (Charge); s = -q                          */
+    double inv_mass;            /* 1/m for a constant mass                      */
+    int mass_axis;              /* -1 = constant mass                           */
+    const double *inv_mass_q;   /* 1/m at the quadrature points of mass_axis    */
+    const double *pot_q[3];     /* V_d at the quadrature points of axis d       */
+    const double *cap_q[3];     /* W_d at the quadrature points of axis d       */
+    double cap_inv_mass;        /* 1/m scale of the CAP (TDSEZCapMassScale)     */
+    int coupled[3];             /* 1 = field couples on this axis (dipole term) */
+    int dirichlet;              /* 1 = homogeneous Dirichlet walls (1D only)    */
+} tdz_physics;
+
+/* ------------------------------------------------------------- operator
+ * Matrix-free operator set of one space and physics: M, H (K + sV + CAP) and
+ * the dipoles D_a as sums of Kronecker products of 1D bands, applied by fused
+ * sm_103a kernels. Replaces the assembled AIJ matrices of
+ * TDSEZCore::Assemble (src/core.cpp:22-105), TDSEZAssembler
+ * (src/assembler_class.cpp:102-272) and the factorised apply of
+ * TDSEZTensorOps::Setup (src/tensorops.cpp:16-81).
+ */
+tdz_status tdz_operator_create(const tdz_space *s, const tdz_physics *phys, tdz_op **out);
+/* Stage coefficients of A = alpha M + g (H + sum_a c_a D_a), c over the
+ * coupled axes in x, y, z order (nc of them, interleaved re/im). Replaces
+ * the value passes BuildStageMatrix / UpdateStageBase / TDSEZFusedStage
+ * (src/propagator.cpp:374-551) and the CN IJacobian J = i a M - H - sum c D
+ * (src/monitor.cpp:294-331, as alpha = -i a, g = 1 up to the sign). Takes
+ * effect for TDZ_STAGE applies issued after the call on any stream. */
+tdz_status tdz_operator_set_stage(tdz_op *op, double alpha_re, double alpha_im, double g_re, double g_im,
+                                  int nc, const double *c);
+/* y = op x. Replaces MatMult on M, H, D_a and the stage matrices
+ * (src/propagator.cpp:622-623, src/monitor.cpp:114-116) and
+ * TDSEZTensorOps::Apply (src/tensorops.cpp:155-188). x and y must not alias. */
+tdz_status tdz_operator_apply(tdz_op *op, int which, int precision, const void *x, void *y, void *stream);
+/* Number of fused-apply kernel launches issued so far by this operator. */
+long long tdz_operator_launches(const tdz_op *op);
+void tdz_operator_destroy(tdz_op *op);
+
+/* --------------------------------------------------------------- solver
+ * FGMRES (FP64, right preconditioned) on the stage operator of an operator
+ * set, with a preconditioner built on the device. Replaces KSPSetOperators /
+ * KSPSolve with the KSP configuration of src/propagator.cpp:125-197,315-370
+ * and the multigrid of TDSEZSetupMultigrid (src/multigrid.cpp:205-327).
+ * The solve stops when ||b - A x|| <= rtol ||b|| (true residual norm of
+ * right-preconditioned FGMRES).
+ */
+typedef struct tdz_solver tdz_solver;
+#define TDZ_PC_NONE 0
+#define TDZ_PC_MASS 1 /* exact Kronecker inverse of the overlap M           */
+#define TDZ_PC_MG 2   /* geometric B-spline multigrid V-cycle               */
+typedef struct tdz_solver_opts {
+    int restart;        /* Krylov restart; 0 = 30, or 50 above 100000 rows   */
+    int maxit;          /* iteration cap; 0 = 1000                           */
+    double rtol;        /* relative residual; 0 = 1e-12                      */
+    int pc;             /* TDZ_PC_*                                          */
+    int pc_precision;   /* TDZ_FP32 (mixed precision) or TDZ_FP64            */
+    int mg_levels;      /* 0 = coarsen until < 2000 DoFs (MGLevels = 0)      */
+    int mg_smooth;      /* Chebyshev degree of pre/post smoothing; 0 = 2     */
+    int mg_coarse_its;  /* Chebyshev degree on the coarsest level; 0 = 12    */
+} tdz_solver_opts;
+/* Set up the solver for the current stage of op (call set_stage first). */
+tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);
+/* Solve A x = b (FP64 device vectors; x holds the initial guess).
+ * its / reason / rnorm may be NULL. reason > 0: converged; < 0: diverged
+ * (PETSc KSPConvergedReason numbering: -3 iteration cap, -9 NaN/Inf). */
+tdz_status tdz_solver_solve(tdz_solver *s, const void *b, void *x, void *stream, int *its, int *reason,
+                            double *rnorm);
+void tdz_solver_destroy(tdz_solver *s);
+
+/* ----------------------------------------------------------- propagator
+ * Time steps of TDSEZPropagator::Evolve (CN, src/propagator.cpp:78-251) and
+ * EvolveRational / Pade22Step (src/propagator.cpp:564-769) on a device state
+ * psi (FP64). Field coefficients are the values c_a = s E_a(t) of the
+ * coupled axes (TDSEZManager::TermCoefficients, src/manager.cpp:1020-1027):
+ *   TDZ_CN, TDZ_PADE22: c1 at t + h/2 (c2 unused)
+ *   TDZ_MAGNUS4:        c1 at t + (1/2 - sqrt3/6) h, c2 at t + (1/2 + sqrt3/6) h
+ * A failed stage solve returns TDZ_ERR_NOT_CONVERGED / TDZ_ERR_BREAKDOWN
+ * (the PetscCheck(reason > 0) of src/propagator.cpp:671-672).
+ */
+typedef struct tdz_prop tdz_prop;
+#define TDZ_CN 0
+#define TDZ_PADE22 1
+#define TDZ_MAGNUS4 2
+tdz_status tdz_prop_create(tdz_op *op, int kind, const tdz_solver_opts *opts, int guess_order, void *stream,
+                           tdz_prop **out);
+tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, const double *c2, void *stream);
+/* Totals: stage solves, Krylov iterations, FP64 operator applies of the
+ * solver, multigrid cycles; last solve's iterations and relative residual. */
+tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies,
+                          long long *cycles, int *last_its, double *last_rres);
+void tdz_prop_destroy(tdz_prop *p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDZ_H */

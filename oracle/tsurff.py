@@ -154,3 +154,40 @@ class OracleTSurff:
         self.prev = cur
         self.prevT = t
         return amp
+
+    def interior(self, psi, kgrid):
+        """Projection of psi(T) inside the box |x_d| < R onto the Volkov states
+        at the last sample time (the SurffInterior term of tdsez_tsurff.hpp,
+        ``Interior``/``Project``, ``src/tsurff.cpp:565-639``): adding it makes
+        the spectrum exact for any final time."""
+        sp_ = self.space
+        ks = [np.asarray(kgrid[d]) for d in range(self.dim)]
+        out = None
+        # separable: psi values on the tensor grid of in-box Gauss points
+        pts, wts, Bs = [], [], []
+        for d in range(self.dim):
+            ax = sp_.axes[d]
+            xs, ws = self.nodes[d], self.weights[d]
+            Bm = np.zeros((len(xs), ax.n))
+            for i, x in enumerate(xs):
+                s = find_span(ax.knots, ax.p, ax.n, x)
+                Bm[i, s - ax.p:s + 1] = ders_basis(ax.knots, ax.p, s, x, 0)[0]
+            pts.append(xs)
+            wts.append(ws)
+            Bs.append(Bm)
+        G = psi.reshape(self.space.shape)
+        for d in range(self.dim):       # contract axis d (x is the last array axis)
+            G = np.moveaxis(np.tensordot(Bs[d], np.moveaxis(G, self.dim - 1 - d, 0), axes=(1, 0)),
+                            0, self.dim - 1 - d)
+        # integrate chi^* psi: factorised over axes
+        for d in range(self.dim):
+            E = np.exp(-1j * np.outer(ks[d] + self.A[d], pts[d])) * wts[d][None, :]
+            G = np.moveaxis(np.tensordot(E, np.moveaxis(G, self.dim - 1 - d, 0), axes=(1, 0)),
+                            0, self.dim - 1 - d)
+        K = np.meshgrid(*reversed(ks), indexing="ij")   # shaped like G (slowest axis first)
+        phi = self.C
+        for d in range(self.dim):
+            kd = K[self.dim - 1 - d]
+            phi = phi + self.vt * kd * kd / (2 * self.mass) + kd * self.B[d] / self.mass
+        out = (2 * math.pi) ** (-0.5 * self.dim) * np.exp(1j * phi) * G
+        return np.moveaxis(out, list(range(self.dim)), list(reversed(range(self.dim)))).reshape(-1)

@@ -1,0 +1,118 @@
+"""ctypes binding of libtdz.so (the C ABI declared in include/tdz.h).
+
+The library is built in-tree by ``tdsez_gb300.build``. Loading fails loudly
+when it is missing: there is no CPU fallback for any operation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libtdz.so"
+
+TDZ_OK = 0
+TDZ_FP32, TDZ_FP64 = 0, 1
+TDZ_MASS, TDZ_HAMILTONIAN, TDZ_DIPOLE_X, TDZ_DIPOLE_Y, TDZ_DIPOLE_Z, TDZ_STAGE = range(6)
+
+STATUS_NAMES = {0: "TDZ_OK", 1: "TDZ_ERR_ARG", 2: "TDZ_ERR_CUDA", 3: "TDZ_ERR_NOT_CONVERGED",
+                4: "TDZ_ERR_STATE", 5: "TDZ_ERR_UNSUPPORTED", 6: "TDZ_ERR_BREAKDOWN", 7: "TDZ_ERR_INTERNAL"}
+
+
+class TDZError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class tdz_physics(C.Structure):
+    _fields_ = [
+        ("charge", C.c_double),
+        ("inv_mass", C.c_double),
+        ("mass_axis", C.c_int),
+        ("inv_mass_q", C.POINTER(C.c_double)),
+        ("pot_q", C.POINTER(C.c_double) * 3),
+        ("cap_q", C.POINTER(C.c_double) * 3),
+        ("cap_inv_mass", C.c_double),
+        ("coupled", C.c_int * 3),
+        ("dirichlet", C.c_int),
+    ]
+
+
+class tdz_solver_opts(C.Structure):
+    _fields_ = [
+        ("restart", C.c_int),
+        ("maxit", C.c_int),
+        ("rtol", C.c_double),
+        ("pc", C.c_int),
+        ("pc_precision", C.c_int),
+        ("mg_levels", C.c_int),
+        ("mg_smooth", C.c_int),
+        ("mg_coarse_its", C.c_int),
+    ]
+
+
+TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG = 0, 1, 2
+TDZ_CN, TDZ_PADE22, TDZ_MAGNUS4 = 0, 1, 2
+
+_lib = None
+
+VP = C.c_void_p
+PP = C.POINTER(C.c_void_p)
+I = C.c_int
+D = C.c_double
+LL = C.c_longlong
+
+# name -> (restype, argtypes); every symbol declared in include/tdz.h
+SIGNATURES = {
+    "tdz_last_error": (C.c_char_p, []),
+    "tdz_version": (C.c_char_p, []),
+    "tdz_space_create": (I, [I, C.POINTER(I), C.POINTER(I), C.POINTER(C.POINTER(D)), I, PP]),
+    "tdz_space_axis": (I, [VP, I, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+    "tdz_space_ndof": (I, [VP, C.POINTER(LL)]),
+    "tdz_space_quadrature": (I, [VP, I, C.POINTER(D), C.POINTER(D)]),
+    "tdz_space_destroy": (None, [VP]),
+    "tdz_operator_create": (I, [VP, C.POINTER(tdz_physics), PP]),
+    "tdz_operator_set_stage": (I, [VP, D, D, D, D, I, C.POINTER(D)]),
+    "tdz_operator_apply": (I, [VP, I, I, VP, VP, VP]),
+    "tdz_operator_launches": (LL, [VP]),
+    "tdz_operator_destroy": (None, [VP]),
+    "tdz_solver_create": (I, [VP, C.c_void_p, VP, PP]),
+    "tdz_solver_solve": (I, [VP, VP, VP, VP, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
+    "tdz_solver_destroy": (None, [VP]),
+    "tdz_prop_create": (I, [VP, I, C.c_void_p, I, VP, PP]),
+    "tdz_prop_step": (I, [VP, VP, D, C.POINTER(D), C.POINTER(D), VP]),
+    "tdz_prop_stats": (I, [VP, C.POINTER(LL), C.POINTER(LL), C.POINTER(LL), C.POINTER(LL), C.POINTER(I),
+                           C.POINTER(D)]),
+    "tdz_prop_destroy": (None, [VP]),
+}
+
+
+def load():
+    """Load libtdz.so (building it first when it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int):
+    if status != TDZ_OK:
+        msg = load().tdz_last_error().decode(errors="replace")
+        raise TDZError(status, msg)
+
+
+def dptr(arr):
+    """POINTER(c_double) of a contiguous float64 numpy array (or None)."""
+    if arr is None:
+        return None
+    return arr.ctypes.data_as(C.POINTER(C.c_double))

@@ -1,0 +1,87 @@
+// Dispatch of the fused apply: stage scalars folded into the kernel
+// parameters, degree-specific instantiations in apply_p<P>.cu.
+#include "apply_kernels.cuh"
+
+#include <type_traits>
+
+namespace tdz {
+
+namespace {
+
+template <class T>
+CombP<T> eval_comb(const Comb &c, const std::array<cd, 5> &sg) {
+    CombP<T> out{};
+    out.n = c.n;
+    for (int i = 0; i < c.n; ++i) {
+        const cd v = c.factor[i] * sg[c.scalar[i]];
+        out.base[i] = c.base[i];
+        out.re[i] = (T)v.real();
+        out.im[i] = (T)v.imag();
+    }
+    return out;
+}
+
+template <class T>
+ApplyParams<T> make_params(const Operator &op, const Plan &pl, const void *x, void *y) {
+    ApplyParams<T> prm{};
+    const Space &s = *op.sp;
+    const bool dbl = std::is_same<T, double>::value;
+    prm.x = x;
+    prm.y = y;
+    prm.n0 = s.ax[0].n;
+    prm.n1 = s.dim > 1 ? s.ax[1].n : 1;
+    prm.n2 = s.dim > 2 ? s.ax[2].n : 1;
+    prm.b0 = static_cast<const T *>((dbl ? op.dev64[0] : op.dev32[0]).ptr);
+    prm.b1 = s.dim > 1 ? static_cast<const T *>((dbl ? op.dev64[1] : op.dev32[1]).ptr) : nullptr;
+    prm.b2 = s.dim > 2 ? static_cast<const T *>((dbl ? op.dev64[2] : op.dev32[2]).ptr) : nullptr;
+    const std::array<cd, 5> sg = op.sigma_for(pl.which);
+    prm.xT = eval_comb<T>(pl.xT, sg);
+    prm.yT = eval_comb<T>(pl.yT, sg);
+    prm.zA = eval_comb<T>(pl.zA, sg);
+    prm.zC = eval_comb<T>(pl.zC, sg);
+    prm.p = s.ax[0].p;
+    prm.walls = 0;
+    if (pl.walls) {
+        prm.walls = 1;
+        for (int w = 0; w < 2; ++w) {
+            cd d = 0;
+            if (pl.wall_m >= 0) d += sg[pl.wall_m] * op.m_wall[w];
+            if (pl.wall_h >= 0) d += sg[pl.wall_h] * op.h_wall[w];
+            prm.wall_re[w] = (T)d.real();
+            prm.wall_im[w] = (T)d.imag();
+        }
+    }
+    return prm;
+}
+
+template <class T>
+void launch_1d(const ApplyParams<T> &prm, cudaStream_t st) {
+    const int threads = 128;
+    k_apply1d<T><<<(prm.n0 + threads - 1) / threads, threads, 0, st>>>(prm);
+}
+
+}  // namespace
+
+void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st) {
+    const bool dbl = prec == TDZ_FP64;
+    const int dim = op.sp->dim;
+    if (dim == 1) {
+        if (dbl) launch_1d(make_params<double>(op, pl, x, y), st);
+        else launch_1d(make_params<float>(op, pl, x, y), st);
+    } else {
+        ApplyParams<float> pf{};
+        ApplyParams<double> pd{};
+        if (dbl) pd = make_params<double>(op, pl, x, y);
+        else pf = make_params<float>(op, pl, x, y);
+        switch (op.P) {
+        case 2: apply_p2(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
+        case 3: apply_p3(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
+        case 4: apply_p4(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
+        case 5: apply_p5(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
+        default: throw Error(TDZ_ERR_UNSUPPORTED, "2D/3D apply supports degrees 2..5");
+        }
+    }
+    TDZ_CUDA(cudaGetLastError());
+}
+
+}  // namespace tdz

@@ -1,0 +1,335 @@
+// Fused matrix-free apply of the three-stream Kronecker form (see oper.h),
+//   y = T_z (x) M_y (x) M_x x                                   stream A
+//     + M_z (x) [M_y (x) T_x + T_y (x) M_x] x                   stream B
+//     + Mm_z (x) [M_y (x) S_x + S_y (x) M_x] x                  stream C
+// on sm_103a. Replaces MatMult on the assembled AIJ stage matrices and the
+// three-pass TDSEZTensorOps::Term (src/tensorops.cpp:97-153).
+//
+// 3D kernel: a CTA owns a TX x TY column tile and streams the z planes of its
+// z chunk. Per input plane it stages the (TY+2p) x (TX+2p) halo tile in
+// shared memory, contracts along x (the band rows of its own column in
+// registers), then along y (shared memory), and feeds the streams into a
+// ring of 2p+1 output-plane accumulators held in registers: plane z
+// contributes Z(m, z) w(z) to output planes m = z-p..z+p (the outer bands
+// are symmetric, so that is row z of Z), and plane z-p is complete and
+// stored once plane z has been added. The complex band combinations are
+// formed from the real base bands and the stage scalars (kernel parameters),
+// so a stage change needs no upload. Every coefficient is read from HBM once
+// per apply (halo re-reads hit L2) and written once.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "cplx.cuh"
+#include "oper.h"
+
+namespace tdz {
+
+template <class T> struct CombP {
+    int n;
+    int base[kMaxComb];
+    T re[kMaxComb], im[kMaxComb];
+};
+
+template <class T> struct ApplyParams {
+    const void *x;
+    void *y;
+    int n0, n1, n2;             // sizes along x, y, z (unused axes 1)
+    const T *b0, *b1, *b2;      // base bands per axis [nbase][n][2p+1]
+    CombP<T> xT, yT, zA, zC;
+    int zchunk;
+    int p;                      // degree (1D kernel)
+    T wall_re[2], wall_im[2];   // 1D walls: diagonal values, wall = 0 / n-1
+    int walls;
+};
+
+// entry o of row i of a combination of base bands
+template <class T, class C>
+__device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, int bw, int i, int o) {
+    C z = czero<C>();
+    for (int t = 0; t < cb.n; ++t) {
+        const T b = bands[((size_t)cb.base[t] * n + i) * bw + o];
+        z.x = fma(cb.re[t], b, z.x);
+        z.y = fma(cb.im[t], b, z.y);
+    }
+    return z;
+}
+
+// ---------------------------------------------------------------- 3D kernel
+template <class T, int P, bool HB, bool HC, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
+    using C = typename CT<T>::type;
+    constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
+    constexpr int NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
+    constexpr int UT = 1, US = HB ? 2 : 1;    // slots of u_T and u_S in sU
+    __shared__ C sIn[RY][RX];
+    __shared__ C sU[NU][RY][TX];
+    __shared__ T sYm[BW][TY];
+    __shared__ T sYs[HC ? BW : 1][TY];
+    __shared__ C sYt[HB ? BW : 1][TY];
+    __shared__ C sZA[BW], sZC[BW];
+    __shared__ T sZM[BW];
+
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int n0 = prm.n0, n1 = prm.n1, n2 = prm.n2;
+    const int tilesX = (n0 + TX - 1) / TX;
+    const int x0 = (blockIdx.x % tilesX) * TX, y0 = (blockIdx.x / tilesX) * TY;
+    const int gx = x0 + tx, gy = y0 + ty;
+    const int z0 = blockIdx.y * prm.zchunk;
+    const int z1 = min(n2, z0 + prm.zchunk);
+    if (z0 >= z1) return;
+    const C *__restrict__ X = static_cast<const C *>(prm.x);
+    C *__restrict__ Y = static_cast<C *>(prm.y);
+
+    // band rows of this thread's x column
+    T xm[BW], xs[HC ? BW : 1];
+    C xt[HB ? BW : 1];
+#pragma unroll
+    for (int j = 0; j < BW; ++j) {
+        const bool in = gx < n0;
+        xm[j] = in ? prm.b0[((size_t)kM * n0 + gx) * BW + j] : T(0);
+        if constexpr (HC) xs[j] = in ? prm.b0[((size_t)kS * n0 + gx) * BW + j] : T(0);
+        if constexpr (HB) xt[j] = in ? comb_at<T, C>(prm.xT, prm.b0, n0, BW, gx, j) : czero<C>();
+    }
+    for (int i = tid; i < BW * TY; i += TX * TY) {
+        const int j = i / TY, r = i % TY, yy = y0 + r;
+        const bool in = yy < n1;
+        sYm[j][r] = in ? prm.b1[((size_t)kM * n1 + yy) * BW + j] : T(0);
+        if constexpr (HC) sYs[j][r] = in ? prm.b1[((size_t)kS * n1 + yy) * BW + j] : T(0);
+        if constexpr (HB) sYt[j][r] = in ? comb_at<T, C>(prm.yT, prm.b1, n1, BW, yy, j) : czero<C>();
+    }
+
+    C acc[BW];
+#pragma unroll
+    for (int s = 0; s < BW; ++s) acc[s] = czero<C>();
+
+    const int zs = z0 - P;
+    const int nplanes = (z1 - z0) + 2 * P;
+    for (int base = 0; base < nplanes; base += BW) {
+#pragma unroll
+        for (int ph = 0; ph < BW; ++ph) {
+            const int it = base + ph;
+            if (it >= nplanes) break;
+            const int zin = zs + it;
+            if (zin >= 0 && zin < n2) {
+                __syncthreads();
+                for (int i = tid; i < RY * RX; i += TX * TY) {
+                    const int r = i / RX, c = i % RX;
+                    const int yy = y0 - P + r, xx = x0 - P + c;
+                    C v = czero<C>();
+                    if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) v = X[((size_t)zin * n1 + yy) * n0 + xx];
+                    sIn[r][c] = v;
+                }
+                if (tid < BW) {
+                    sZA[tid] = comb_at<T, C>(prm.zA, prm.b2, n2, BW, zin, tid);
+                    if constexpr (HB) sZM[tid] = prm.b2[((size_t)kM * n2 + zin) * BW + tid];
+                    if constexpr (HC) sZC[tid] = comb_at<T, C>(prm.zC, prm.b2, n2, BW, zin, tid);
+                }
+                __syncthreads();
+                // x stage
+                for (int r = ty; r < RY; r += TY) {
+                    C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
+#pragma unroll
+                    for (int j = 0; j < BW; ++j) {
+                        const C v = sIn[r][tx + j];
+                        rfma(uM, xm[j], v);
+                        if constexpr (HB) cfma(uT, xt[j], v);
+                        if constexpr (HC) rfma(uS, xs[j], v);
+                    }
+                    sU[0][r][tx] = uM;
+                    if constexpr (HB) sU[UT][r][tx] = uT;
+                    if constexpr (HC) sU[US][r][tx] = uS;
+                }
+                __syncthreads();
+                // y stage
+                C wA = czero<C>(), wB = czero<C>(), wC = czero<C>();
+#pragma unroll
+                for (int j = 0; j < BW; ++j) {
+                    const T ym = sYm[j][ty];
+                    const C um = sU[0][ty + j][tx];
+                    rfma(wA, ym, um);
+                    if constexpr (HB) {
+                        rfma(wB, ym, sU[UT][ty + j][tx]);
+                        cfma(wB, sYt[j][ty], um);
+                    }
+                    if constexpr (HC) {
+                        rfma(wC, ym, sU[US][ty + j][tx]);
+                        rfma(wC, sYs[j][ty], um);
+                    }
+                }
+                // outer (z) stage
+#pragma unroll
+                for (int o = 0; o < BW; ++o) {
+                    C &a = acc[(ph - P + o + 2 * BW) % BW];
+                    cfma(a, sZA[o], wA);
+                    if constexpr (HB) rfma(a, sZM[o], wB);
+                    if constexpr (HC) cfma(a, sZC[o], wC);
+                }
+            }
+            if (it >= 2 * P) {
+                const int m = zin - P;
+                if (gx < n0 && gy < n1) Y[((size_t)m * n1 + gy) * n0 + gx] = acc[(ph - P + 2 * BW) % BW];
+            }
+            acc[(ph - P + 2 * BW) % BW] = czero<C>();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- 2D kernel
+// x stage on a TX-wide row tile, outer stage along y with the register ring.
+template <class T, int P, bool HB, bool HC, int TX>
+__global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
+    using C = typename CT<T>::type;
+    constexpr int BW = 2 * P + 1, RX = TX + 2 * P;
+    __shared__ C sIn[RX];
+    __shared__ C sZA[BW], sZC[BW];
+    __shared__ T sZM[BW];
+    const int tx = threadIdx.x;
+    const int n0 = prm.n0, n1 = prm.n1;
+    const int x0 = blockIdx.x * TX, gx = x0 + tx;
+    const int z0 = blockIdx.y * prm.zchunk;
+    const int z1 = min(n1, z0 + prm.zchunk);
+    if (z0 >= z1) return;
+    const C *__restrict__ X = static_cast<const C *>(prm.x);
+    C *__restrict__ Y = static_cast<C *>(prm.y);
+    T xm[BW], xs[HC ? BW : 1];
+    C xt[HB ? BW : 1];
+#pragma unroll
+    for (int j = 0; j < BW; ++j) {
+        const bool in = gx < n0;
+        xm[j] = in ? prm.b0[((size_t)kM * n0 + gx) * BW + j] : T(0);
+        if constexpr (HC) xs[j] = in ? prm.b0[((size_t)kS * n0 + gx) * BW + j] : T(0);
+        if constexpr (HB) xt[j] = in ? comb_at<T, C>(prm.xT, prm.b0, n0, BW, gx, j) : czero<C>();
+    }
+    C acc[BW];
+#pragma unroll
+    for (int s = 0; s < BW; ++s) acc[s] = czero<C>();
+    const int zs = z0 - P;
+    const int nplanes = (z1 - z0) + 2 * P;
+    for (int base = 0; base < nplanes; base += BW) {
+#pragma unroll
+        for (int ph = 0; ph < BW; ++ph) {
+            const int it = base + ph;
+            if (it >= nplanes) break;
+            const int zin = zs + it;
+            if (zin >= 0 && zin < n1) {
+                __syncthreads();
+                for (int c = tx; c < RX; c += TX) {
+                    const int xx = x0 - P + c;
+                    sIn[c] = (xx >= 0 && xx < n0) ? X[(size_t)zin * n0 + xx] : czero<C>();
+                }
+                if (tx < BW) {
+                    sZA[tx] = comb_at<T, C>(prm.zA, prm.b1, n1, BW, zin, tx);
+                    if constexpr (HB) sZM[tx] = prm.b1[((size_t)kM * n1 + zin) * BW + tx];
+                    if constexpr (HC) sZC[tx] = comb_at<T, C>(prm.zC, prm.b1, n1, BW, zin, tx);
+                }
+                __syncthreads();
+                C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
+#pragma unroll
+                for (int j = 0; j < BW; ++j) {
+                    const C v = sIn[tx + j];
+                    rfma(uM, xm[j], v);
+                    if constexpr (HB) cfma(uT, xt[j], v);
+                    if constexpr (HC) rfma(uS, xs[j], v);
+                }
+#pragma unroll
+                for (int o = 0; o < BW; ++o) {
+                    C &a = acc[(ph - P + o + 2 * BW) % BW];
+                    cfma(a, sZA[o], uM);
+                    if constexpr (HB) rfma(a, sZM[o], uT);
+                    if constexpr (HC) cfma(a, sZC[o], uS);
+                }
+            }
+            if (it >= 2 * P) {
+                const int m = zin - P;
+                if (gx < n0) Y[(size_t)m * n0 + gx] = acc[(ph - P + 2 * BW) % BW];
+            }
+            acc[(ph - P + 2 * BW) % BW] = czero<C>();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- 1D kernel
+template <class T>
+__global__ void k_apply1d(const ApplyParams<T> prm) {
+    using C = typename CT<T>::type;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = prm.n0, p = prm.p, bw = 2 * p + 1;
+    if (i >= n) return;
+    const C *__restrict__ X = static_cast<const C *>(prm.x);
+    C *__restrict__ Y = static_cast<C *>(prm.y);
+    const bool wall_i = prm.walls && (i == 0 || i == n - 1);
+    C acc = czero<C>();
+    if (wall_i) {
+        const int s = i == 0 ? 0 : 1;
+        C d;
+        d.x = prm.wall_re[s];
+        d.y = prm.wall_im[s];
+        cfma(acc, d, X[i]);
+    } else {
+        for (int o = 0; o < bw; ++o) {
+            const int j = i - p + o;
+            if (j < 0 || j >= n) continue;
+            if (prm.walls && (j == 0 || j == n - 1)) continue;
+            cfma(acc, comb_at<T, C>(prm.zA, prm.b0, n, bw, i, o), X[j]);
+        }
+    }
+    Y[i] = acc;
+}
+
+// ---------------------------------------------------------------- launch helpers
+constexpr int kTX3 = 32, kTY3 = 8, kTX2 = 128;
+
+inline int pick_chunk(int tiles, int n_outer, int P) {
+    // about 8 CTAs per SM over 152 SMs; chunks no shorter than 4p planes
+    const int target = 152 * 8;
+    int chunks = (target + tiles - 1) / tiles;
+    chunks = std::max(1, std::min(chunks, n_outer / std::max(1, 4 * P)));
+    return (n_outer + chunks - 1) / chunks;
+}
+
+template <class T, int P, bool HB, bool HC>
+inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
+    ApplyParams<T> prm = prm0;
+    const int tiles = ((prm.n0 + kTX3 - 1) / kTX3) * ((prm.n1 + kTY3 - 1) / kTY3);
+    prm.zchunk = pick_chunk(tiles, prm.n2, P);
+    dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
+    k_apply3d<T, P, HB, HC, kTX3, kTY3><<<grid, dim3(kTX3, kTY3), 0, st>>>(prm);
+}
+
+template <class T, int P, bool HB, bool HC>
+inline void run2d(const ApplyParams<T> &prm0, cudaStream_t st) {
+    ApplyParams<T> prm = prm0;
+    const int tiles = (prm.n0 + kTX2 - 1) / kTX2;
+    prm.zchunk = pick_chunk(tiles, prm.n1, P);
+    dim3 grid(tiles, (prm.n1 + prm.zchunk - 1) / prm.zchunk);
+    k_apply2d<T, P, HB, HC, kTX2><<<grid, kTX2, 0, st>>>(prm);
+}
+
+template <class T, int P>
+inline void dispatch_streams(int dim, bool hb, bool hc, const ApplyParams<T> &prm, cudaStream_t st) {
+    if (dim == 3) {
+        if (hb && hc) run3d<T, P, true, true>(prm, st);
+        else if (hb) run3d<T, P, true, false>(prm, st);
+        else if (hc) run3d<T, P, false, true>(prm, st);
+        else run3d<T, P, false, false>(prm, st);
+    } else {
+        if (hb && hc) run2d<T, P, true, true>(prm, st);
+        else if (hb) run2d<T, P, true, false>(prm, st);
+        else if (hc) run2d<T, P, false, true>(prm, st);
+        else run2d<T, P, false, false>(prm, st);
+    }
+}
+
+// per-degree entry points (apply_p<P>.cu)
+#define TDZ_APPLY_DECL(P)                                                                                  \
+    void apply_p##P(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd, \
+                    bool dbl, cudaStream_t st);
+TDZ_APPLY_DECL(2)
+TDZ_APPLY_DECL(3)
+TDZ_APPLY_DECL(4)
+TDZ_APPLY_DECL(5)
+#undef TDZ_APPLY_DECL
+
+}  // namespace tdz

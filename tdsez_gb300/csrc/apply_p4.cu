@@ -1,0 +1,12 @@
+// Instantiations of the fused 2D/3D apply kernels for degree 4.
+#include "apply_kernels.cuh"
+
+namespace tdz {
+
+void apply_p4(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd, bool dbl,
+              cudaStream_t st) {
+    if (dbl) dispatch_streams<double, 4>(dim, hb, hc, pd, st);
+    else dispatch_streams<float, 4>(dim, hb, hc, pf, st);
+}
+
+}  // namespace tdz

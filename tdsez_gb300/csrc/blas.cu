@@ -1,0 +1,291 @@
+// Device vector operations for the Krylov solvers. Reductions (dot products
+// and norms) accumulate in FP64 with warp-shuffle + shared-memory block sums
+// into per-block partials, then one block per result sums the partials in a
+// fixed order: the result does not depend on scheduling (bit-reproducible).
+#include "blas.h"
+
+#include <algorithm>
+
+#include "cplx.cuh"
+
+namespace tdz {
+namespace blas {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRedBlocks = 2 * 152;
+
+inline int grid_for(size_t n) {
+    const size_t b = (n + kThreads - 1) / kThreads;
+    return (int)std::min<size_t>(std::max<size_t>(b, 1), 8 * 152);
+}
+
+template <class C> __device__ __forceinline__ C cmk(double re, double im) {
+    C c;
+    c.x = re;
+    c.y = im;
+    return c;
+}
+
+template <class T>
+__global__ void k_scale(typename CT<T>::type *x, double ar, double ai, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        auto v = x[i];
+        const T re = (T)ar * v.x - (T)ai * v.y, im = (T)ar * v.y + (T)ai * v.x;
+        v.x = re;
+        v.y = im;
+        x[i] = v;
+    }
+}
+
+template <class T>
+__global__ void k_axpbypcz(typename CT<T>::type *y, double ar, double ai, const typename CT<T>::type *x, double br,
+                           double bi, const typename CT<T>::type *z, double cr, double ci, size_t n) {
+    using C = typename CT<T>::type;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        C acc = czero<C>();
+        if (ar != 0.0 || ai != 0.0) cfma(acc, cmk<C>(ar, ai), x[i]);
+        if (br != 0.0 || bi != 0.0) cfma(acc, cmk<C>(br, bi), y[i]);
+        if (z && (cr != 0.0 || ci != 0.0)) cfma(acc, cmk<C>(cr, ci), z[i]);
+        y[i] = acc;
+    }
+}
+
+__global__ void k_cast64to32(const double2 *x, float2 *y, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = x[i];
+        y[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+__global__ void k_cast32to64(const float2 *x, double2 *y, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = x[i];
+        y[i] = make_double2(v.x, v.y);
+    }
+}
+
+__global__ void k_add_cast(double2 *y, double ar, double ai, const float2 *x, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = x[i];
+        double2 w = y[i];
+        w.x += ar * v.x - ai * v.y;
+        w.y += ar * v.y + ai * v.x;
+        y[i] = w;
+    }
+}
+
+struct PtrPack {
+    const void *p[kMaxDot];
+};
+struct CoefPack {
+    double re[kMaxDot], im[kMaxDot];
+};
+
+// per-block partial sums of conj(V_i) w, i < k; partial layout [i][block]
+template <class T, int K>
+__global__ void __launch_bounds__(kThreads) k_mdot(PtrPack V, const typename CT<T>::type *w, size_t n,
+                                                   double2 *partial) {
+    using C = typename CT<T>::type;
+    double2 acc[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) acc[i] = make_double2(0.0, 0.0);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const C wv = w[e];
+        const double wr = wv.x, wi = wv.y;
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            const C v = static_cast<const C *>(V.p[i])[e];
+            const double vr = v.x, vi = v.y;
+            acc[i].x += vr * wr + vi * wi;
+            acc[i].y += vr * wi - vi * wr;
+        }
+    }
+    __shared__ double2 red[kThreads / 32][K];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        double re = acc[i].x, im = acc[i].y;
+        for (int off = 16; off > 0; off >>= 1) {
+            re += __shfl_down_sync(0xffffffffu, re, off);
+            im += __shfl_down_sync(0xffffffffu, im, off);
+        }
+        if (lane == 0) red[warp][i] = make_double2(re, im);
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double re = 0.0, im = 0.0;
+        for (int w2 = 0; w2 < kThreads / 32; ++w2) { re += red[w2][threadIdx.x].x; im += red[w2][threadIdx.x].y; }
+        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_double2(re, im);
+    }
+}
+
+// result[i] = sum over blocks of partial[i][block] (one block per i, fixed order)
+__global__ void k_finish(const double2 *partial, int blocks, double2 *result) {
+    __shared__ double2 red[kThreads];
+    const int i = blockIdx.x;
+    double re = 0.0, im = 0.0;
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) {
+        re += partial[(size_t)i * blocks + b].x;
+        im += partial[(size_t)i * blocks + b].y;
+    }
+    red[threadIdx.x] = make_double2(re, im);
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            red[threadIdx.x].x += red[threadIdx.x + s].x;
+            red[threadIdx.x].y += red[threadIdx.x + s].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) result[i] = red[0];
+}
+
+template <class T, int K>
+__global__ void k_maxpy(typename CT<T>::type *w, PtrPack V, CoefPack a, size_t n) {
+    using C = typename CT<T>::type;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        C acc = w[e];
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            const C v = static_cast<const C *>(V.p[i])[e];
+            acc.x += (T)a.re[i] * v.x - (T)a.im[i] * v.y;
+            acc.y += (T)a.re[i] * v.y + (T)a.im[i] * v.x;
+        }
+        w[e] = acc;
+    }
+}
+
+template <class T, int K>
+void mdot_k(const PtrPack &pp, const void *w, size_t n, double2 *partial, int blocks, cudaStream_t st) {
+    k_mdot<T, K><<<blocks, kThreads, 0, st>>>(pp, static_cast<const typename CT<T>::type *>(w), n, partial);
+}
+
+template <class T>
+void mdot_dispatch(int k, const PtrPack &pp, const void *w, size_t n, double2 *partial, int blocks,
+                   cudaStream_t st) {
+    switch (k) {
+#define TDZ_CASE(K) case K: mdot_k<T, K>(pp, w, n, partial, blocks, st); break;
+        TDZ_CASE(1) TDZ_CASE(2) TDZ_CASE(3) TDZ_CASE(4) TDZ_CASE(5) TDZ_CASE(6) TDZ_CASE(7) TDZ_CASE(8)
+        TDZ_CASE(9) TDZ_CASE(10) TDZ_CASE(11) TDZ_CASE(12) TDZ_CASE(13) TDZ_CASE(14) TDZ_CASE(15) TDZ_CASE(16)
+#undef TDZ_CASE
+    default: throw Error(TDZ_ERR_INTERNAL, "bad multi-dot width");
+    }
+}
+
+template <class T>
+void maxpy_dispatch(int k, void *w, const PtrPack &pp, const CoefPack &cp, size_t n, cudaStream_t st) {
+    using C = typename CT<T>::type;
+    C *wp = static_cast<C *>(w);
+    const int g = grid_for(n);
+    switch (k) {
+#define TDZ_CASE(K) case K: k_maxpy<T, K><<<g, kThreads, 0, st>>>(wp, pp, cp, n); break;
+        TDZ_CASE(1) TDZ_CASE(2) TDZ_CASE(3) TDZ_CASE(4) TDZ_CASE(5) TDZ_CASE(6) TDZ_CASE(7) TDZ_CASE(8)
+        TDZ_CASE(9) TDZ_CASE(10) TDZ_CASE(11) TDZ_CASE(12) TDZ_CASE(13) TDZ_CASE(14) TDZ_CASE(15) TDZ_CASE(16)
+#undef TDZ_CASE
+    default: throw Error(TDZ_ERR_INTERNAL, "bad multi-axpy width");
+    }
+}
+
+}  // namespace
+
+void copy(const void *x, void *y, size_t n, int prec, cudaStream_t st) {
+    const size_t bytes = n * (prec == TDZ_FP64 ? 16 : 8);
+    if (x != y) TDZ_CUDA(cudaMemcpyAsync(y, x, bytes, cudaMemcpyDeviceToDevice, st));
+}
+
+void zero(void *x, size_t n, int prec, cudaStream_t st) {
+    TDZ_CUDA(cudaMemsetAsync(x, 0, n * (prec == TDZ_FP64 ? 16 : 8), st));
+}
+
+void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
+    const int g = grid_for(n);
+    if (prec == TDZ_FP64) k_scale<double><<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), a.real(), a.imag(), n);
+    else k_scale<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(x), a.real(), a.imag(), n);
+    TDZ_CUDA(cudaGetLastError());
+}
+
+void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st) {
+    const int g = grid_for(n);
+    if (prec == TDZ_FP64)
+        k_axpbypcz<double><<<g, kThreads, 0, st>>>(static_cast<double2 *>(y), a.real(), a.imag(),
+                                                   static_cast<const double2 *>(x), b.real(), b.imag(),
+                                                   static_cast<const double2 *>(z), c.real(), c.imag(), n);
+    else
+        k_axpbypcz<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(y), a.real(), a.imag(),
+                                                  static_cast<const float2 *>(x), b.real(), b.imag(),
+                                                  static_cast<const float2 *>(z), c.real(), c.imag(), n);
+    TDZ_CUDA(cudaGetLastError());
+}
+
+void axpby(void *y, cd a, const void *x, cd b, size_t n, int prec, cudaStream_t st) {
+    axpbypcz(y, a, x, b, nullptr, 0.0, n, prec, st);
+}
+
+void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st) {
+    const int g = grid_for(n);
+    if (px == py) { copy(x, y, n, px, st); return; }
+    if (px == TDZ_FP64) k_cast64to32<<<g, kThreads, 0, st>>>(static_cast<const double2 *>(x), static_cast<float2 *>(y), n);
+    else k_cast32to64<<<g, kThreads, 0, st>>>(static_cast<const float2 *>(x), static_cast<double2 *>(y), n);
+    TDZ_CUDA(cudaGetLastError());
+}
+
+void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
+    k_add_cast<<<grid_for(n), kThreads, 0, st>>>(y, a.real(), a.imag(), x, n);
+    TDZ_CUDA(cudaGetLastError());
+}
+
+void Reducer::init() {
+    if (blocks) return;
+    blocks = kRedBlocks;
+    partial.alloc(sizeof(double2) * kMaxDot * blocks);
+    result.alloc(sizeof(double2) * kMaxDot);
+    TDZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host), sizeof(double2) * kMaxDot));
+}
+
+Reducer::~Reducer() {
+    if (host) cudaFreeHost(host);
+}
+
+void mdot(Reducer &r, const void *const *V, int k, const void *w, size_t n, int prec, cd *out, cudaStream_t st) {
+    r.init();
+    for (int c0 = 0; c0 < k; c0 += kMaxDot) {
+        const int kk = std::min(kMaxDot, k - c0);
+        PtrPack pp{};
+        for (int i = 0; i < kk; ++i) pp.p[i] = V[c0 + i];
+        if (prec == TDZ_FP64) mdot_dispatch<double>(kk, pp, w, n, r.partial.as<double2>(), r.blocks, st);
+        else mdot_dispatch<float>(kk, pp, w, n, r.partial.as<double2>(), r.blocks, st);
+        k_finish<<<kk, kThreads, 0, st>>>(r.partial.as<double2>(), r.blocks, r.result.as<double2>());
+        TDZ_CUDA(cudaGetLastError());
+        TDZ_CUDA(cudaMemcpyAsync(r.host, r.result.ptr, sizeof(double2) * kk, cudaMemcpyDeviceToHost, st));
+        TDZ_CUDA(cudaStreamSynchronize(st));
+        for (int i = 0; i < kk; ++i) out[c0 + i] = cd(r.host[i].x, r.host[i].y);
+    }
+}
+
+void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st) {
+    for (int c0 = 0; c0 < k; c0 += kMaxDot) {
+        const int kk = std::min(kMaxDot, k - c0);
+        PtrPack pp{};
+        CoefPack cp{};
+        for (int i = 0; i < kk; ++i) {
+            pp.p[i] = V[c0 + i];
+            cp.re[i] = a[c0 + i].real();
+            cp.im[i] = a[c0 + i].imag();
+        }
+        if (prec == TDZ_FP64) maxpy_dispatch<double>(kk, w, pp, cp, n, st);
+        else maxpy_dispatch<float>(kk, w, pp, cp, n, st);
+        TDZ_CUDA(cudaGetLastError());
+    }
+}
+
+double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st) {
+    cd v;
+    const void *V[1] = {x};
+    mdot(r, V, 1, x, n, prec, &v, st);
+    return std::sqrt(std::max(0.0, v.real()));
+}
+
+}  // namespace blas
+}  // namespace tdz

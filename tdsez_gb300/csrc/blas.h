@@ -1,0 +1,47 @@
+// Device vector operations on interleaved complex arrays (FP32 / FP64), with
+// deterministic FP64 reductions. Internal to the tdz library.
+#pragma once
+
+#include "common.h"
+
+namespace tdz {
+namespace blas {
+
+constexpr int kMaxDot = 16;   // vectors per fused multi-dot / multi-axpy pass
+
+// y = x
+void copy(const void *x, void *y, size_t n, int prec, cudaStream_t st);
+// x = 0
+void zero(void *x, size_t n, int prec, cudaStream_t st);
+// x *= a
+void scale(void *x, cd a, size_t n, int prec, cudaStream_t st);
+// y = a x + b y
+void axpby(void *y, cd a, const void *x, cd b, size_t n, int prec, cudaStream_t st);
+// y = a x + b y + c z
+void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st);
+// y (precision py) = x (precision px)
+void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st);
+// y64 += a * x32 (FP32 correction added to an FP64 vector)
+void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st);
+
+// Reduction workspace: per-block partial sums and device results.
+struct Reducer {
+    DevBuf partial;   // [kMaxDot][blocks] double2
+    DevBuf result;    // [kMaxDot] double2
+    DevBuf hostbuf;   // pinned host mirror of result
+    double2 *host = nullptr;
+    int blocks = 0;
+    void init();
+    ~Reducer();
+};
+
+// out[i] = <V_i, w> = sum conj(V_i) w for i < k (any k; chunks of kMaxDot),
+// precision prec; results copied to the host (synchronises the stream).
+void mdot(Reducer &r, const void *const *V, int k, const void *w, size_t n, int prec, cd *out, cudaStream_t st);
+// w += sum_i a_i V_i
+void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st);
+// ||x||_2 (synchronises)
+double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st);
+
+}  // namespace blas
+}  // namespace tdz

@@ -1,0 +1,54 @@
+// Flexible GMRES in FP64 on the device with a pluggable preconditioner.
+// Internal to the tdz library.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "blas.h"
+#include "oper.h"
+
+namespace tdz {
+
+// z = P^-1 r on FP64 vectors (a preconditioner may work in FP32 inside).
+struct Precond {
+    virtual ~Precond() = default;
+    virtual void apply(const double2 *r, double2 *z, cudaStream_t st) = 0;
+    virtual void refresh() {}   // rebuild from the current stage operator
+    virtual long long launches() const { return 0; }
+};
+
+struct PcNone : Precond {
+    size_t n;
+    explicit PcNone(size_t n_) : n(n_) {}
+    void apply(const double2 *r, double2 *z, cudaStream_t st) override { blas::copy(r, z, n, TDZ_FP64, st); }
+};
+
+struct SolveStats {
+    int its = 0;           // iterations of the last solve
+    int reason = 0;        // > 0 converged, < 0 diverged (PETSc KSPConvergedReason convention)
+    double rnorm = 0.0;    // final residual estimate (absolute)
+    double bnorm = 0.0;
+};
+
+// FGMRES(m), right preconditioned, classical Gram-Schmidt with one
+// re-orthogonalisation (two fused passes per iteration), Givens rotations on
+// the host. Replaces KSPFGMRES/KSPGMRES with PC_RIGHT of
+// src/propagator.cpp:125-197,315-370 (stop when ||b - A x|| <= rtol ||b||).
+struct FGMRES {
+    Operator *op = nullptr;
+    size_t n = 0;
+    int restart = 30;
+    Precond *pc = nullptr;
+    std::vector<DevBuf> V, Z;
+    DevBuf w;
+    blas::Reducer red;
+    SolveStats last;
+    long long applies = 0;
+
+    void setup(Operator *op_, int restart_, Precond *pc_);
+    // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.
+    SolveStats solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st);
+};
+
+}  // namespace tdz

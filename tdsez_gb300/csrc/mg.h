@@ -1,0 +1,80 @@
+// Geometric B-spline multigrid on the device. Internal to the tdz library.
+//
+// Hierarchy as TDSEZSetupMultigrid (src/multigrid.cpp:205-263): coarse
+// knots drop every other simple interior breakpoint, C0 knots stay; the
+// prolongation is Boehm knot insertion per axis (multigrid.cpp:52-81),
+// applied as a tensor product; coarse operators are the Galerkin products
+// P^T A P, formed exactly per axis on the 1D bands (P_d^T B P_d), so every
+// level is applied by the same fused kernels and follows stage changes
+// without a rebuild. Smoother: Chebyshev iteration in M^-1 A on the
+// spectral segment alpha + g [mu_lo, mu_hi] of the stage (M^-1 by exact
+// Kronecker line solves); coarsest level: Chebyshev over the whole segment.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "blas.h"
+#include "krylov.h"
+#include "linesolve.h"
+#include "oper.h"
+
+namespace tdz {
+
+// Row-sparse 1D matrix with a fixed row width (prolongation and its transpose).
+struct RowSparse {
+    int rows = 0, cols = 0, width = 0;
+    std::vector<int> col;      // rows * width (-1 = empty)
+    std::vector<double> val;
+    DevBuf dcol, dval32, dval64;
+    void upload();
+};
+
+struct MGLevel {
+    Space space;                          // sizes of the level
+    std::unique_ptr<Operator> op;         // level operator (bands = Galerkin products)
+    Operator *opp = nullptr;              // op.get() or the fine operator
+    KronSolve minv;
+    RowSparse P[3], R[3];                 // to this level from the next coarser: prolongation, restriction
+    int n[3] = {1, 1, 1};
+    size_t ndof = 0;
+    DevBuf x, b, r, d, z, t1, t2;         // working precision vectors
+    double mu_lo = 0.0, mu_hi = 0.0;      // spectrum of M^-1 H_E on this level
+};
+
+struct MGOptions {
+    int levels = 0;          // 0 = until < 2000 DoFs (MGLevels = 0)
+    int smooth = 2;          // Chebyshev degree of pre and post smoothing
+    int coarse_its = 12;     // Chebyshev degree of the coarsest solve
+    double ratio = 6.0;      // smoothing range [mu_hi / ratio, mu_hi]
+    int precision = TDZ_FP32;
+};
+
+struct Multigrid : Precond {
+    Operator *fine = nullptr;
+    MGOptions opt;
+    std::vector<MGLevel> lv;
+    int prec = TDZ_FP32;
+    DevBuf in32;                          // FP32 copy of the FP64 input
+    long long cycles = 0;
+    blas::Reducer red;
+
+    void setup(Operator *fine_, const MGOptions &o, cudaStream_t st);
+    void estimate_bounds(cudaStream_t st);
+    void vcycle(int l, cudaStream_t st);  // lv[l].b -> lv[l].x
+    void apply(const double2 *r, double2 *z, cudaStream_t st) override;
+    void refresh() override;
+};
+
+// 1D helpers (mg_setup.cpp)
+std::vector<double> coarsen_knots(const std::vector<double> &U, bool *dropped);
+int count_spans(const std::vector<double> &U);
+// dense-free Boehm prolongation as sparse rows: fine n_f x coarse n_c
+RowSparse boehm_prolongation(const std::vector<double> &C, const std::vector<double> &F, int p);
+RowSparse transpose(const RowSparse &P);
+BandD galerkin(const RowSparse &P, const BandD &B);   // P^T B P (banded, coarse)
+// axis contraction out = A (along axis) in, with optional accumulation (mg.cu)
+void axis_contract(const RowSparse &A, int axis, const void *in, void *out, int n0, int n1, int n2, bool accumulate,
+                   int prec, cudaStream_t st);
+
+}  // namespace tdz

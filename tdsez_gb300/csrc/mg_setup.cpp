@@ -1,0 +1,366 @@
+// Multigrid hierarchy, Galerkin bands and the V-cycle (host orchestration).
+#include <algorithm>
+#include <cmath>
+#include <utility>
+
+#include "mg.h"
+
+namespace tdz {
+
+// ---------------------------------------------------------------- 1D pieces
+std::vector<double> coarsen_knots(const std::vector<double> &U, bool *dropped) {
+    // breakpoints with multiplicity; drop every other simple interior one
+    std::vector<std::pair<double, int>> bp;
+    for (double u : U) {
+        if (!bp.empty() && u == bp.back().first) ++bp.back().second;
+        else bp.push_back({u, 1});
+    }
+    std::vector<double> C;
+    *dropped = false;
+    for (size_t i = 0; i < bp.size(); ++i) {
+        const bool interior = i > 0 && i + 1 < bp.size();
+        if (interior && bp[i].second == 1 && i % 2 == 1) { *dropped = true; continue; }
+        C.insert(C.end(), bp[i].second, bp[i].first);
+    }
+    return C;
+}
+
+int count_spans(const std::vector<double> &U) {
+    int n = 0;
+    for (size_t i = 0; i + 1 < U.size(); ++i)
+        if (U[i + 1] > U[i]) ++n;
+    return n;
+}
+
+RowSparse boehm_prolongation(const std::vector<double> &C, const std::vector<double> &F, int p) {
+    using Row = std::vector<std::pair<int, double>>;
+    std::vector<double> U = C;
+    const int nc = (int)C.size() - p - 1;
+    std::vector<Row> P(nc);
+    for (int j = 0; j < nc; ++j) P[j] = {{j, 1.0}};
+    // knots of F missing from C (multiset difference of sorted lists)
+    std::vector<double> add;
+    {
+        size_t i = 0, j = 0;
+        while (i < F.size()) {
+            if (j < C.size() && C[j] == F[i]) { ++i; ++j; }
+            else if (j < C.size() && C[j] < F[i]) ++j;
+            else add.push_back(F[i++]);
+        }
+    }
+    auto combine = [](const Row &a, double wa, const Row &b, double wb) {
+        Row out;
+        size_t i = 0, j = 0;
+        while (i < a.size() || j < b.size()) {
+            if (j >= b.size() || (i < a.size() && a[i].first < b[j].first)) { out.push_back({a[i].first, wa * a[i].second}); ++i; }
+            else if (i >= a.size() || b[j].first < a[i].first) { out.push_back({b[j].first, wb * b[j].second}); ++j; }
+            else { out.push_back({a[i].first, wa * a[i].second + wb * b[j].second}); ++i; ++j; }
+        }
+        return out;
+    };
+    for (double xi : add) {
+        const int n = (int)U.size() - p - 1;
+        int k = (int)(std::upper_bound(U.begin(), U.end(), xi) - U.begin()) - 1;
+        k = std::min(std::max(k, p), n - 1);
+        std::vector<Row> Q(n + 1);
+        for (int i = 0; i <= k - p; ++i) Q[i] = P[i];
+        for (int i = k + 1; i <= n; ++i) Q[i] = P[i - 1];
+        for (int i = k - p + 1; i <= k; ++i) {
+            const double a = (xi - U[i]) / (U[i + p] - U[i]);
+            Q[i] = combine(P[i], a, P[i - 1], 1.0 - a);
+        }
+        P.swap(Q);
+        U.insert(std::upper_bound(U.begin(), U.end(), xi), xi);
+    }
+    RowSparse R;
+    R.rows = (int)P.size();
+    R.cols = nc;
+    for (auto &r : P) {
+        r.erase(std::remove_if(r.begin(), r.end(), [](const auto &e) { return std::abs(e.second) < 1e-14; }), r.end());
+        R.width = std::max(R.width, (int)r.size());
+    }
+    R.col.assign((size_t)R.rows * R.width, -1);
+    R.val.assign((size_t)R.rows * R.width, 0.0);
+    for (int i = 0; i < R.rows; ++i)
+        for (size_t t = 0; t < P[i].size(); ++t) {
+            R.col[(size_t)i * R.width + t] = P[i][t].first;
+            R.val[(size_t)i * R.width + t] = P[i][t].second;
+        }
+    return R;
+}
+
+RowSparse transpose(const RowSparse &P) {
+    std::vector<std::vector<std::pair<int, double>>> rows(P.cols);
+    for (int i = 0; i < P.rows; ++i)
+        for (int t = 0; t < P.width; ++t) {
+            const int j = P.col[(size_t)i * P.width + t];
+            if (j >= 0) rows[j].push_back({i, P.val[(size_t)i * P.width + t]});
+        }
+    RowSparse R;
+    R.rows = P.cols;
+    R.cols = P.rows;
+    for (auto &r : rows) R.width = std::max(R.width, (int)r.size());
+    R.col.assign((size_t)R.rows * R.width, -1);
+    R.val.assign((size_t)R.rows * R.width, 0.0);
+    for (int j = 0; j < R.rows; ++j)
+        for (size_t t = 0; t < rows[j].size(); ++t) {
+            R.col[(size_t)j * R.width + t] = rows[j][t].first;
+            R.val[(size_t)j * R.width + t] = rows[j][t].second;
+        }
+    return R;
+}
+
+void RowSparse::upload() {
+    tdz::upload(dcol, col);
+    tdz::upload(dval64, val);
+    std::vector<float> v32(val.begin(), val.end());
+    tdz::upload(dval32, v32);
+}
+
+BandD galerkin(const RowSparse &P, const BandD &B) {
+    const int p = B.p;
+    BandD Cb(P.cols, p);
+    for (int i = 0; i < P.rows; ++i)
+        for (int j = std::max(0, i - p); j <= std::min(P.rows - 1, i + p); ++j) {
+            const double bij = B.at(i, j);
+            if (bij == 0.0) continue;
+            for (int s = 0; s < P.width; ++s) {
+                const int k = P.col[(size_t)i * P.width + s];
+                if (k < 0) break;
+                const double pik = P.val[(size_t)i * P.width + s] * bij;
+                for (int t = 0; t < P.width; ++t) {
+                    const int l = P.col[(size_t)j * P.width + t];
+                    if (l < 0) break;
+                    TDZ_CHECK(std::abs(k - l) <= p, TDZ_ERR_INTERNAL, "Galerkin product leaves the band");
+                    Cb.at(k, l) += pik * P.val[(size_t)j * P.width + t];
+                }
+            }
+        }
+    return Cb;
+}
+
+// ---------------------------------------------------------------- hierarchy
+void Multigrid::setup(Operator *fine_, const MGOptions &o, cudaStream_t st) {
+    fine = fine_;
+    opt = o;
+    prec = o.precision;
+    const Space &fs = *fine->sp;
+    const int dim = fs.dim;
+    TDZ_CHECK(!fine->wall1d, TDZ_ERR_UNSUPPORTED, "multigrid with Dirichlet walls is not supported");
+    const int p = fs.ax[0].p;
+    // knot hierarchy, finest first
+    std::vector<std::array<std::vector<double>, 3>> K(1);
+    for (int d = 0; d < dim; ++d) K[0][d] = fs.ax[d].U;
+    const int maxLevels = opt.levels > 0 ? opt.levels : 20;
+    while ((int)K.size() < maxLevels) {
+        auto C = K.back();
+        bool any = false;
+        long long dofs = 1;
+        for (int d = 0; d < dim; ++d) {
+            bool dropped = false;
+            auto Cd = coarsen_knots(K.back()[d], &dropped);
+            if (dropped && count_spans(Cd) >= p + 1) { C[d] = Cd; any = true; }
+            dofs *= (long long)C[d].size() - p - 1;
+        }
+        if (!any) break;
+        K.push_back(C);
+        if (opt.levels == 0 && dofs < 2000) break;
+    }
+    const int L = (int)K.size();
+    lv.clear();
+    lv.resize(L);
+    for (int l = 0; l < L; ++l) {
+        MGLevel &m = lv[l];
+        if (l == 0) {
+            m.space = fs;
+            m.opp = fine;
+        } else {
+            m.space.dim = dim;
+            m.space.nquad = fs.nquad;
+            for (int d = 0; d < dim; ++d) {
+                const auto &U = K[l][d];
+                m.space.ax[d].setup(U.data(), (int)U.size(), p, std::max(1, std::min(fs.nquad, 2)));
+            }
+            // Galerkin operator from the next finer level
+            const Operator &fo = *lv[l - 1].opp;
+            auto op = std::make_unique<Operator>();
+            op->space = m.space;
+            op->sp = &op->space;
+            op->phys = fo.phys;
+            op->P = p;
+            op->terms = fo.terms;
+            op->coupled = fo.coupled;
+            op->sigma = fo.sigma;
+            op->stage_set = true;
+            for (int d = 0; d < dim; ++d) {
+                m.P[d] = boehm_prolongation(K[l][d], K[l - 1][d], p);
+                m.R[d] = transpose(m.P[d]);
+                m.P[d].upload();
+                m.R[d].upload();
+                for (const BandD &b : fo.bases[d]) op->bases[d].push_back(galerkin(m.P[d], b));
+            }
+            op->upload_bases();
+            m.opp = op.get();
+            m.op = std::move(op);
+        }
+        for (int d = 0; d < 3; ++d) m.n[d] = d < dim ? m.space.ax[d].n : 1;
+        m.ndof = (size_t)m.space.ndof();
+        std::array<const BandD *, 3> mb{nullptr, nullptr, nullptr};
+        for (int d = 0; d < dim; ++d) mb[d] = &m.opp->bases[d][kM];
+        m.minv.setup(mb, dim);
+        const size_t es = prec == TDZ_FP64 ? sizeof(double2) : sizeof(float2);
+        for (DevBuf *b : {&m.x, &m.b, &m.r, &m.d, &m.z, &m.t1, &m.t2}) b->alloc(m.ndof * es);
+    }
+    red.init();
+    estimate_bounds(st);
+}
+
+namespace {
+// deterministic pseudo-random start vector for the power iterations
+void fill_start(DevBuf &v, size_t n, int prec, cudaStream_t st) {
+    std::vector<double> h(2 * n);
+    uint64_t s = 0x9e3779b97f4a7c15ull;
+    for (size_t i = 0; i < 2 * n; ++i) {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        h[i] = (double)(s >> 11) / (double)(1ull << 53) - 0.5;
+    }
+    if (prec == TDZ_FP64) TDZ_CUDA(cudaMemcpyAsync(v.ptr, h.data(), h.size() * 8, cudaMemcpyHostToDevice, st));
+    else {
+        std::vector<float> f(h.begin(), h.end());
+        TDZ_CUDA(cudaMemcpyAsync(v.ptr, f.data(), f.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    TDZ_CUDA(cudaStreamSynchronize(st));
+}
+}  // namespace
+
+void Multigrid::estimate_bounds(cudaStream_t st) {
+    // field coefficients of the current stage: sigma[2+k] = g c_k
+    const std::array<cd, 5> sg = fine->sigma;
+    std::vector<cd> c;
+    for (size_t k = 0; k < fine->coupled.size(); ++k)
+        c.push_back(std::abs(sg[1]) > 0 ? sg[2 + k] / sg[1] : cd(0));
+    for (auto &m : lv) {
+        Operator &op = *m.opp;
+        const auto saved = op.sigma;
+        op.set_stage(0.0, 1.0, c);          // H_E
+        fill_start(m.x, m.ndof, prec, st);
+        double lam = 0.0;
+        // largest eigenvalue of M^-1 H_E
+        for (int it = 0; it < 40; ++it) {
+            op.apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
+            m.minv.apply(m.t1.ptr, prec, st);
+            const double nx = blas::nrm2(red, m.x.ptr, m.ndof, prec, st);
+            const double nt = blas::nrm2(red, m.t1.ptr, m.ndof, prec, st);
+            lam = nt / std::max(nx, 1e-300);
+            blas::axpby(m.x.ptr, cd(1.0 / std::max(nt, 1e-300)), m.t1.ptr, 0.0, m.ndof, prec, st);
+        }
+        m.mu_hi = 1.05 * lam;
+        // lowest: largest eigenvalue of mu_hi - M^-1 H_E
+        fill_start(m.x, m.ndof, prec, st);
+        double lam2 = 0.0;
+        for (int it = 0; it < 40; ++it) {
+            op.apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
+            m.minv.apply(m.t1.ptr, prec, st);
+            blas::axpby(m.t1.ptr, cd(m.mu_hi), m.x.ptr, -1.0, m.ndof, prec, st);
+            const double nx = blas::nrm2(red, m.x.ptr, m.ndof, prec, st);
+            const double nt = blas::nrm2(red, m.t1.ptr, m.ndof, prec, st);
+            lam2 = nt / std::max(nx, 1e-300);
+            blas::axpby(m.x.ptr, cd(1.0 / std::max(nt, 1e-300)), m.t1.ptr, 0.0, m.ndof, prec, st);
+        }
+        m.mu_lo = m.mu_hi - 1.05 * lam2;
+        op.sigma = saved;
+    }
+}
+
+void Multigrid::refresh() {}
+
+namespace {
+
+// Chebyshev iteration on A x = b with M^-1, spectral segment
+// alpha + g [mu_a, mu_b]; x_zero: x starts at 0.
+void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, int steps, bool x_zero, cudaStream_t st) {
+    Operator &op = *m.opp;
+    const cd alpha = op.sigma[0], g = op.sigma[1];
+    const cd theta = alpha + g * (0.5 * (mu_a + mu_b));
+    const cd delta = g * (0.5 * (mu_b - mu_a));
+    const size_t n = m.ndof;
+    // r = b - A x
+    if (x_zero) blas::copy(m.b.ptr, m.r.ptr, n, prec, st);
+    else {
+        op.apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
+        blas::axpbypcz(m.r.ptr, 1.0, m.b.ptr, 0.0, m.t1.ptr, -1.0, n, prec, st);
+    }
+    const cd sigma1 = theta / delta;
+    cd rho = 1.0 / sigma1;
+    blas::copy(m.r.ptr, m.z.ptr, n, prec, st);
+    m.minv.apply(m.z.ptr, prec, st);
+    blas::axpby(m.d.ptr, 1.0 / theta, m.z.ptr, 0.0, n, prec, st);
+    if (x_zero) blas::copy(m.d.ptr, m.x.ptr, n, prec, st);
+    else blas::axpby(m.x.ptr, 1.0, m.d.ptr, 1.0, n, prec, st);
+    for (int k = 1; k < steps; ++k) {
+        op.apply(TDZ_STAGE, prec, m.d.ptr, m.t1.ptr, st);
+        blas::axpby(m.r.ptr, -1.0, m.t1.ptr, 1.0, n, prec, st);
+        blas::copy(m.r.ptr, m.z.ptr, n, prec, st);
+        m.minv.apply(m.z.ptr, prec, st);
+        const cd rn = 1.0 / (2.0 * sigma1 - rho);
+        blas::axpby(m.d.ptr, 2.0 * rn / delta, m.z.ptr, rn * rho, n, prec, st);
+        blas::axpby(m.x.ptr, 1.0, m.d.ptr, 1.0, n, prec, st);
+        rho = rn;
+    }
+}
+
+}  // namespace
+
+void Multigrid::vcycle(int l, cudaStream_t st) {
+    MGLevel &m = lv[l];
+    const int last = (int)lv.size() - 1;
+    if (l == last) {
+        chebyshev(m, prec, m.mu_lo, m.mu_hi, opt.coarse_its, true, st);
+        return;
+    }
+    const double lo = m.mu_hi / opt.ratio;
+    chebyshev(m, prec, lo, m.mu_hi, opt.smooth, true, st);
+    // r = b - A x
+    m.opp->apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
+    blas::axpbypcz(m.r.ptr, 1.0, m.b.ptr, 0.0, m.t1.ptr, -1.0, m.ndof, prec, st);
+    // restrict: axis 2, then 1, then 0 (shrinking early)
+    MGLevel &c = lv[l + 1];
+    const int dim = m.space.dim;
+    int sh[3] = {m.n[0], m.n[1], m.n[2]};
+    const void *src = m.r.ptr;
+    void *tmp[2] = {m.t1.ptr, m.t2.ptr};
+    int ti = 0;
+    for (int d = dim - 1; d >= 0; --d) {
+        void *dst = d == 0 ? c.b.ptr : tmp[ti];
+        axis_contract(c.R[d], d, src, dst, sh[0], sh[1], sh[2], false, prec, st);
+        sh[d] = c.n[d];
+        src = dst;
+        ti ^= 1;
+    }
+    vcycle(l + 1, st);
+    // prolongate and add: axis 0, 1, 2 (growing late)
+    int s2[3] = {c.n[0], c.n[1], c.n[2]};
+    src = c.x.ptr;
+    ti = 0;
+    for (int d = 0; d < dim; ++d) {
+        const bool lastp = d == dim - 1;
+        void *dst = lastp ? m.x.ptr : tmp[ti];
+        axis_contract(c.P[d], d, src, dst, s2[0], s2[1], s2[2], lastp, prec, st);
+        s2[d] = m.n[d];
+        src = dst;
+        ti ^= 1;
+    }
+    chebyshev(m, prec, lo, m.mu_hi, opt.smooth, false, st);
+}
+
+void Multigrid::apply(const double2 *r, double2 *z, cudaStream_t st) {
+    // coarse levels follow the current stage scalars of the fine operator
+    for (size_t l = 1; l < lv.size(); ++l) lv[l].opp->sigma = fine->sigma;
+    MGLevel &f = lv[0];
+    blas::cast(r, TDZ_FP64, f.b.ptr, prec, f.ndof, st);
+    vcycle(0, st);
+    blas::cast(f.x.ptr, prec, z, TDZ_FP64, f.ndof, st);
+    ++cycles;
+}
+
+}  // namespace tdz

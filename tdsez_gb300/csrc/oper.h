@@ -1,0 +1,83 @@
+// Matrix-free operator: Kronecker terms, compiled apply plans and device
+// copies of the bands. Internal to the tdz library.
+#pragma once
+
+#include <array>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "space.h"
+
+namespace tdz {
+
+constexpr int kMaxComb = 8;   // base bands in one combination
+
+// coef * (band[2] (x) band[1] (x) band[0]); band ids index the per-axis base
+// band lists of the operator. The coefficient is factor * sigma[scalar] with
+// sigma = (alpha, g, g c_0, g c_1, g c_2) of the current stage.
+struct Term {
+    int scalar;
+    cd factor;
+    std::array<int, 3> band;
+};
+
+// Linear combination sum_i factor_i sigma[scalar_i] B_{base_i} of base bands
+// of one axis; evaluated into kernel parameters at every launch.
+struct Comb {
+    int n = 0;
+    std::array<int, kMaxComb> base{}, scalar{};
+    std::array<cd, kMaxComb> factor{};
+    void add(int b, int s, cd f);
+};
+
+// Three-stream form of every operator of the hot path (outer axis = last):
+//   stream A:  T_out (x) M (x) M                       one-axis terms of the outer axis and alpha M
+//   stream B:  M_out (x) [M_y (x) T_x + T_y (x) M_x]    one-axis terms of the inner axes
+//   stream C:  Mm_out (x) [M_y (x) S_x + S_y (x) M_x]   kinetic terms of a mass layered
+//                                                       along the outer axis
+// T_x, T_y, T_out and the stream-C outer coefficient are combinations of
+// real base bands with complex stage scalars. In 1D everything is stream A.
+struct Plan {
+    int which = 0, dim = 0;
+    bool hasA = false, hasB = false, hasC = false;
+    Comb xT, yT, zA, zC;
+    bool walls = false;                         // 1D Dirichlet walls pinned in this plan
+    int wall_m = -1, wall_h = -1;               // 1D walls: sigma index of M / H diagonal
+};
+
+struct Operator {
+    const Space *sp = nullptr;
+    Space space;                                // private copy
+    tdz_physics phys{};
+    int P = 0;                                  // common degree (2D/3D kernels)
+    std::array<std::vector<BandD>, 3> bases;    // base bands per axis
+    std::array<DevBuf, 3> dev32, dev64;         // base bands on the device per axis
+    std::vector<Term> terms;                    // all terms of the stage operator
+    std::vector<int> coupled;                   // coupled axes in order
+    // 1D Dirichlet walls: wall diagonal of H and M
+    bool wall1d = false;
+    double h_wall[2] = {0, 0}, m_wall[2] = {0, 0};
+    std::array<cd, 5> sigma{};                  // current stage scalars
+    bool stage_set = false;
+    std::map<int, std::unique_ptr<Plan>> plans; // by TDZ_* operator id
+    long long launches = 0;
+
+    void build(const Space &s, const tdz_physics &ph);
+    int add_band(int axis, BandD b);
+    void upload_bases();
+    std::vector<Term> terms_for(int which) const;
+    std::array<cd, 5> sigma_for(int which) const;
+    Plan &plan(int which);                      // build on first use
+    void compile(Plan &pl, const std::vector<Term> &ts) const;
+    void set_stage(cd alpha, cd g, const std::vector<cd> &c);
+    void apply(int which, int prec, const void *x, void *y, cudaStream_t st);
+};
+
+// base band ids present on every axis
+enum BaseId { kM = 0, kS = 1, kX = 2 };
+
+// kernel launchers (apply.cu)
+void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st);
+
+}  // namespace tdz

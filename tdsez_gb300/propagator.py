@@ -1,0 +1,140 @@
+"""Host side of the GPU stage solves and time steppers.
+
+``Solver`` mirrors the stage KSP of ``TDSEZConfigureStageKSP``
+(``src/propagator.cpp:315-370``); ``Propagator`` mirrors
+``TDSEZPropagator::Evolve`` (Crank-Nicolson) and ``EvolveRational``
+(Pade(2,2), Magnus-4) of ``src/propagator.cpp:78-769``: step times
+t_k = k dt, the last step shortened to end exactly at FinalTime, field
+coefficients c_a = s E_a(t) of the coupled axes, and a monitor callback
+after every step (``TDSEZMonitorStep``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Callable, Optional, Sequence
+
+from . import _lib
+from .operators import Operator
+
+KINDS = {"cn": _lib.TDZ_CN, "pade22": _lib.TDZ_PADE22, "magnus4": _lib.TDZ_MAGNUS4}
+PCS = {"none": _lib.TDZ_PC_NONE, "mass": _lib.TDZ_PC_MASS, "mg": _lib.TDZ_PC_MG}
+S3 = math.sqrt(3.0)
+MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
+
+
+def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
+                maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 2, mg_coarse_its: int = 12):
+    o = _lib.tdz_solver_opts()
+    o.restart = restart
+    o.maxit = maxit
+    o.rtol = rtol
+    o.pc = PCS[pc]
+    o.pc_precision = _lib.TDZ_FP32 if precision == "fp32" else _lib.TDZ_FP64
+    o.mg_levels = mg_levels
+    o.mg_smooth = mg_smooth
+    o.mg_coarse_its = mg_coarse_its
+    return o
+
+
+def _stream(stream):
+    import torch
+    return torch.cuda.current_stream().cuda_stream if stream is None else stream
+
+
+class Solver:
+    """FGMRES + preconditioner on the current stage of ``op``."""
+
+    def __init__(self, op: Operator, stream=None, **kw):
+        self.op = op
+        self.opts = solver_opts(**kw)
+        h = C.c_void_p()
+        _lib.check(_lib.load().tdz_solver_create(op.handle, C.byref(self.opts), C.c_void_p(_stream(stream)),
+                                                 C.byref(h)))
+        self.handle = h
+
+    def solve(self, b, x, stream=None):
+        its, reason, rn = C.c_int(), C.c_int(), C.c_double()
+        _lib.check(_lib.load().tdz_solver_solve(self.handle, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+                                                C.c_void_p(_stream(stream)), C.byref(its), C.byref(reason),
+                                                C.byref(rn)))
+        return its.value, reason.value, rn.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().tdz_solver_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+class Propagator:
+    """Crank-Nicolson / Pade(2,2) / Magnus-4 on the GPU.
+
+    ``field(t)`` returns the physical field E_a(t) of the coupled axes; the
+    coefficients handed to the library are s E_a(t), s = -Charge."""
+
+    def __init__(self, op: Operator, kind: str = "cn", field: Optional[Callable[[float], Sequence[float]]] = None,
+                 guess_order: int = 3, stream=None, **kw):
+        self.op = op
+        self.kind = kind
+        self.field = field or (lambda t: [0.0] * len(op.coupled))
+        self.sign = op.phys.sign
+        self.opts = solver_opts(**kw)
+        h = C.c_void_p()
+        _lib.check(_lib.load().tdz_prop_create(op.handle, KINDS[kind], C.byref(self.opts), guess_order,
+                                               C.c_void_p(_stream(stream)), C.byref(h)))
+        self.handle = h
+
+    def coeffs(self, t: float):
+        return [self.sign * e for e in self.field(t)]
+
+    def step(self, psi, t: float, h: float, stream=None):
+        """One step from t to t + h on the complex128 CUDA tensor psi (in place)."""
+        nc = len(self.op.coupled)
+        arr = C.c_double * max(1, nc)
+        if self.kind == "magnus4":
+            c1 = arr(*self.coeffs(t + MAGNUS_C[0] * h))
+            c2 = arr(*self.coeffs(t + MAGNUS_C[1] * h))
+        else:
+            c1 = arr(*self.coeffs(t + 0.5 * h))
+            c2 = None
+        _lib.check(_lib.load().tdz_prop_step(self.handle, C.c_void_p(psi.data_ptr()), h, c1, c2,
+                                             C.c_void_p(_stream(stream))))
+        return psi
+
+    def evolve(self, psi, dt: float, final_time: float, monitor=None, stream=None):
+        """Steps t_k = k dt, the last one shortened to end at final_time
+        (``src/propagator.cpp:734-741``); ``monitor(step, t, psi)`` after
+        every step and at t = 0."""
+        n = int(math.ceil(final_time / dt - 1e-9))
+        if monitor:
+            monitor(0, 0.0, psi)
+        for step in range(n):
+            t1 = final_time if step + 1 == n else (step + 1) * dt
+            h = t1 - step * dt
+            if abs(h - dt) <= 1e-12 * dt:
+                h = dt
+            self.step(psi, step * dt, h, stream)
+            if monitor:
+                monitor(step + 1, t1, psi)
+        return psi
+
+    def stats(self):
+        s, i, a, cy, li = C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_longlong(), C.c_int()
+        rr = C.c_double()
+        _lib.check(_lib.load().tdz_prop_stats(self.handle, C.byref(s), C.byref(i), C.byref(a), C.byref(cy),
+                                              C.byref(li), C.byref(rr)))
+        return {"solves": s.value, "its": i.value, "applies": a.value, "cycles": cy.value,
+                "last_its": li.value, "last_rres": rr.value}
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().tdz_prop_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

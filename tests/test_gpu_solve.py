@@ -1,0 +1,139 @@
+"""GPU stage solves and time steps against the oracle (direct sparse solves
+of the assembled FP64 matrices), through the C ABI."""
+import math
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as sla
+
+from tests.cases import CASES, oracle_of, product_of
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_const_mass_cap", "2d_cap_softcore_sep", "3d_p2_hole"])
+@pytest.mark.parametrize("pc,prec", [("mg", "fp32"), ("mg", "fp64"), ("mass", "fp32"), ("mass", "fp64")])
+def test_stage_solve_parity(cuda, name, pc, prec):
+    """FGMRES + (mixed-precision) preconditioner reaches the FP64 solution of
+    (M + i tau H_E) x = b: true residual of the oracle matrix <= 1e-11."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    tau = 0.2
+    cc = [0.02 * (k + 1) for k in range(len(c["coupled"]))]
+    op.set_stage(1.0, 1j * tau, cc)
+    Am = (A.M + 1j * tau * (A.H_total() + sum(ck * T for ck, T in zip(cc, A.terms())))).tocsc()
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    xref = sla.spsolve(Am, b)
+    s = Solver(op, pc=pc, precision=prec, rtol=1e-12, maxit=400)
+    bd = torch.tensor(b, device=cuda)
+    xd = torch.zeros_like(bd)
+    its, reason, rn = s.solve(bd, xd)
+    x = xd.cpu().numpy()
+    assert reason > 0, (its, reason, rn)
+    assert np.linalg.norm(b - Am @ x) / np.linalg.norm(b) < 1e-11
+    assert _rel(x, xref) < 1e-9
+    if pc == "mg":
+        assert its <= 60, its
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["3d_heterostructure", "2d_cap_softcore_sep", "3d_const_mass_cap"])
+@pytest.mark.parametrize("kind", ["cn", "pade22", "magnus4"])
+def test_propagation_parity(cuda, name, kind):
+    """Several steps with a time-dependent field: GPU state == oracle state."""
+    import torch
+    from oracle.propagate import OraclePropagator
+    from tdsez_gb300.propagator import Propagator
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    ncpl = len(c["coupled"])
+    field = lambda t: [0.05 * math.sin(0.3 * t + k) for k in range(ncpl)]
+    rng = np.random.default_rng(9)
+    psi0 = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    psi0 /= math.sqrt(np.vdot(psi0, A.M @ psi0).real)
+    P = OraclePropagator(A, field, kind)
+    G = Propagator(op, kind, field=field, pc="mg", precision="fp32", rtol=1e-12)
+    dt = 0.1
+    psi = psi0.copy()
+    pd = torch.tensor(psi0, device=cuda)
+    for step in range(6):
+        psi = P.step(psi, step * dt, dt)
+        G.step(pd, step * dt, dt)
+    assert _rel(pd.cpu().numpy(), psi) < 1e-9
+    st = G.stats()
+    assert st["solves"] == 6 * {"cn": 1, "pade22": 2, "magnus4": 4}[kind]
+    assert st["last_rres"] <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,dt,order,tol", [("cn", 0.02, 2.0, 2e-3), ("magnus4", 0.2, 4.0, 2e-4)])
+def test_driven_oscillator_gpu(cuda, kind, dt, order, tol):
+    """Driven harmonic oscillator (test_analytic.py:226-273) on the GPU:
+    accuracy against the coherent-state <x>(t), observed order, norm 1e-9."""
+    import torch
+    from oracle import bspline as ob
+    from oracle import operators as oo
+    from oracle.propagate import ground_state
+    from tdsez_gb300 import _lib
+    from tdsez_gb300.operators import Operator, Physics
+    from tdsez_gb300.propagator import Propagator
+    from tdsez_gb300.space import Space
+    kn = ob.uniform_knots(120, -20.0, 20.0, 7)
+    A = oo.Assembled(ob.Space([ob.Axis(kn, 7, 10)]), oo.Physics(dim=1, potential=lambda x, y, z: 0.5 * x * x))
+    _, V = ground_state(A)
+    S = Space([kn], 7, 10)
+    op = Operator(S, Physics(potential=[lambda x: 0.5 * x * x], coupled=(0,)))
+    xex = lambda t: -0.5 / (1 - 0.36) * (np.cos(0.6 * t) - np.cos(t))
+    errs, norms = [], []
+    for h in (dt, dt / 2):
+        G = Propagator(op, kind, field=lambda t: [0.5 * math.cos(0.6 * t)], pc="mg", precision="fp32")
+        psi = torch.tensor(V[:, 0], device=cuda)
+        dx = torch.empty_like(psi)
+        mx = torch.empty_like(psi)
+        out = []
+
+        def mon(step, t, p):
+            op.apply(_lib.TDZ_DIPOLE_X, p, dx)
+            op.apply(_lib.TDZ_MASS, p, mx)
+            out.append((t, torch.vdot(p, dx).real.item(), torch.vdot(p, mx).real.item()))
+        G.evolve(psi, h, 10.0, mon)
+        o = np.array(out)
+        errs.append(np.max(np.abs(o[:, 1] - xex(o[:, 0]))))
+        norms.append(np.max(np.abs(o[:, 2] - 1)))
+    assert errs[0] < tol
+    assert abs(math.log2(errs[0] / errs[1]) - order) < 0.3
+    assert max(norms) < 1e-9
+
+
+@pytest.mark.gpu
+def test_failed_solve_is_a_status(cuda):
+    """A stage solve that cannot converge returns TDZ_ERR_NOT_CONVERGED (the
+    PetscCheck(reason > 0) of propagator.cpp:671-672); a NaN state returns a
+    breakdown status. The failure is made on the host: an iteration cap of 1
+    and a NaN input, no device fault."""
+    import torch
+    from tdsez_gb300 import _lib
+    from tdsez_gb300.propagator import Propagator
+    c = CASES["3d_heterostructure"]()
+    PS, op = product_of(c)
+    G = Propagator(op, "cn", field=lambda t: [0.0], pc="none", maxit=1, rtol=1e-14)
+    psi = torch.randn(PS.ndof, dtype=torch.complex128, device=cuda)
+    with pytest.raises(_lib.TDZError) as e:
+        G.step(psi, 0.0, 0.5)
+    assert e.value.status == 3
+    G2 = Propagator(op, "cn", field=lambda t: [0.0], pc="mass")
+    psi[5] = float("nan")
+    with pytest.raises(_lib.TDZError) as e:
+        G2.step(psi, 0.0, 0.5)
+    assert e.value.status == 6
+    # the library stays usable afterwards
+    psi = torch.randn(PS.ndof, dtype=torch.complex128, device=cuda)
+    G2.step(psi, 0.0, 0.5)

@@ -1,0 +1,144 @@
+"""The oracle against the reference's own analytic pins (tests/test_analytic.py,
+tests/test_tsurff.py, tests/test_tensorops.py, tests/test_multigrid.py of the
+TDSE-Z tree): closed forms and exact transfer-matrix energies."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg as la
+
+from oracle import bspline as ob
+from oracle import multigrid as omg
+from oracle import operators as oo
+from oracle import propagate as op
+from oracle import tsurff as ots
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+PINS = json.load(open(os.path.join(GOLDEN, "analytic_pins.json")))
+
+
+def _eig(A, k):
+    E = la.eigh(A.H.toarray(), A.M.toarray(), eigvals_only=True)
+    return np.sort(E)[:k]
+
+
+def test_infinite_well():
+    """E_n = n^2 pi^2 / (2 L^2), Dirichlet walls, p = 7 (test_analytic.py:113-133)."""
+    ax = ob.Axis(ob.uniform_knots(30, 0.0, 10.0, 7), 7, 10)
+    A = oo.Assembled(ob.Space([ax]), oo.Physics(dim=1, potential=lambda x, y, z: 0.0, dirichlet=True))
+    E = _eig(A, 4)
+    exact = np.array(PINS["infinite_well"]["E"])
+    assert np.max(np.abs(E - exact) / exact) < 1e-11
+
+
+def test_double_quantum_well():
+    """GaAs/AlGaAs double well with interface knots: exact BDD energies to
+    1e-8 meV (test_analytic.py:193-219)."""
+    pin = PINS["double_quantum_well"]
+    NM = 18.8973
+    a, b, L = 2 * NM, 10 * NM, 15 * NM
+    mw, mb, V0 = 0.067, 0.0879, 0.00893
+    mf = lambda x, y, z: 1.0 / (mb if abs(x) < a else (mw if abs(x) < b else mb))
+    vf = lambda x, y, z: V0 if abs(x) < a else (0.0 if abs(x) < b else V0)
+    ax = ob.Axis(ob.interface_knots(-L, L, 199, 7, [-b, -a, a, b]), 7, 9)
+    A = oo.Assembled(ob.Space([ax]), oo.Physics(dim=1, potential=vf, inv_mass=mf, mass_const=None))
+    E = _eig(A, 2) * pin["hartree_mev"]
+    assert np.max(np.abs(E - np.array(pin["E_meV"]))) < 1e-8
+
+
+@pytest.mark.parametrize("bc", ["Dirichlet", "Neumann"])
+def test_mass_step(bc):
+    """Mass step m = 1 | 4 with C0 interface knots (test_analytic.py:159-190)."""
+    ax = ob.Axis(ob.interface_knots(-1.0, 1.0, 11, 7, [0.0]), 7, 10)
+    ph = oo.Physics(dim=1, potential=lambda x, y, z: 0.0, inv_mass=lambda x, y, z: 1.0 if x < 0 else 0.25,
+                    mass_const=None, dirichlet=(bc == "Dirichlet"))
+    E = _eig(oo.Assembled(ob.Space([ax]), ph), 3)
+    pin = PINS["mass_step"][bc]
+    assert np.max(np.abs(E[:2] - np.array(pin["E"][:2]))) < 1e-10
+    assert abs(E[2] - pin["E"][2]) < 1e-8
+
+
+@pytest.mark.parametrize("kind,dt,order,tol", [("cn", 0.02, 2.0, 2e-3), ("magnus4", 0.2, 4.0, 2e-4)])
+def test_driven_oscillator(kind, dt, order, tol):
+    """Coherent state of the driven oscillator: accuracy, observed order and
+    norm (test_analytic.py:226-273; p = 7, 200 elements on [-20, 20])."""
+    ax = ob.Axis(ob.uniform_knots(120, -20.0, 20.0, 7), 7, 10)
+    A = oo.Assembled(ob.Space([ax]), oo.Physics(dim=1, potential=lambda x, y, z: 0.5 * x * x))
+    _, V = op.ground_state(A)
+    xex = lambda t: -0.5 / (1 - 0.36) * (np.cos(0.6 * t) - np.cos(t))
+    errs, norms = [], []
+    for h in (dt, dt / 2):
+        P = op.OraclePropagator(A, lambda t: [0.5 * np.cos(0.6 * t)], kind)
+        _, out = P.evolve(V[:, 0], h, 10.0, lambda t, psi: (t, op.expect(A.D[0], psi).real,
+                                                             op.expect(A.M, psi).real))
+        out = np.array(out)
+        errs.append(np.max(np.abs(out[:, 1] - xex(out[:, 0]))))
+        norms.append(np.max(np.abs(out[:, 2] - 1)))
+    assert errs[0] < tol
+    assert abs(math.log2(errs[0] / errs[1]) - order) < 0.3
+    assert max(norms) < 1e-9
+
+
+def test_kron_equals_assembled():
+    """Factorised (Kronecker) apply == assembled quadrature operator
+    (test_tensorops.py:93-102, TDSEZTensorOps::Validate at 1e-10)."""
+    from tests.cases import CASES, oracle_of
+    for name in ("3d_heterostructure", "3d_const_mass_cap", "2d_cap_softcore_sep"):
+        c = CASES[name]()
+        S, ph, A = oracle_of(c)
+        g, cc = 0.3 + 0.7j, [0.05 * (k + 1) for k in range(len(c["coupled"]))]
+        terms = oo.kron_terms(S, ph, g=g, c=cc)
+        x = np.random.default_rng(3).standard_normal(S.ndof) * (1 + 0.5j)
+        ref = A.M @ x + g * (A.H_total() @ x + sum(ck * (T @ x) for ck, T in zip(cc, A.terms())))
+        y = oo.kron_apply(S, terms, x)
+        assert np.abs(y - ref).max() <= 1e-12 * np.abs(ref).max(), name
+
+
+@pytest.mark.parametrize("knots,p", [
+    (ob.uniform_knots(16, -1.0, 1.0, 3), 3),
+    (ob.interface_knots(-12.0, 12.0, 15, 3, [-3.0, 2.0]), 3),
+    (ob.symexp_knots(-60.0, 60.0, 31, 0.9, 4), 4),
+])
+def test_prolongation_exact(knots, p):
+    """Partition of unity and linear precision of the Boehm prolongation
+    (multigrid.cpp:280-293, 1e-10)."""
+    C, dropped = omg.coarsen_knots(knots)
+    assert dropped
+    P = omg.prolongation(C, knots, p)
+    assert np.abs(P.sum(1) - 1).max() < 1e-10
+    assert np.abs(P @ omg.greville(C, p) - omg.greville(knots, p)).max() < 1e-10
+    # C0 interface knots survive coarsening
+    for u in set(knots):
+        if list(knots).count(u) == p and u not in (knots[0], knots[-1]):
+            assert list(C).count(u) == p
+
+
+def test_tsurff_free_packet():
+    """Free Gaussian packet, deck FREE1D of test_tsurff.py:20-52 (p = 7, 400
+    elements on [-40, 40], Pade(2,2) dt = 0.025, T = 20, R = 10, CAP kmin 0.5):
+    |b(k)|^2 against prod (2w^2/pi)^1/2 exp(-2w^2(k-k0)^2) at 1e-4 with the
+    interior term (test_tsurff.py:82-90)."""
+    p, L = 7, 40.0
+    ax = ob.Axis(ob.uniform_knots(400, -L, L, p), p, 10)
+    S = ob.Space([ax])
+    A = oo.Assembled(S, oo.Physics(dim=1, potential=None, cap_kmin=0.5, bounds=[(-L, L)]))
+    w, k0 = 1.0, 2.0
+    g = lambda x: (2 * np.pi * w * w) ** -0.25 * np.exp(-x * x / (4 * w * w) + 1j * k0 * x)
+    b = S.axes[0].basis_matrix(0).T @ (S.axes[0].wq.reshape(-1) * g(S.axes[0].xq.reshape(-1)))
+    import scipy.sparse.linalg as sla
+    psi = sla.spsolve(A.M.tocsc(), b)
+    dt, T = 0.025, 20.0
+    P = op.OraclePropagator(A, lambda t: [0.0], "pade22")
+    ks = np.linspace(-1.0, 5.0, 61)
+    ts = ots.OracleTSurff(S, 10.0, [ks], 1.0, 0.0, 1.0, lambda t: [0.0, 0.0, 0.0], dt)
+    amp = np.zeros(len(ks), dtype=complex)
+    amp = ts.add_flux(0.0, psi, [ks], amp)
+    n = int(round(T / dt))
+    for i in range(n):
+        psi = P.step(psi, i * dt, dt)
+        amp = ts.add_flux((i + 1) * dt, psi, [ks], amp)
+    ex = (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ks - k0) ** 2)
+    tot = amp + ts.interior(psi, [ks])
+    assert np.abs(np.abs(tot) ** 2 - ex).max() / ex.max() < 1e-4
