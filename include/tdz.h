@@ -50,6 +50,9 @@ const char *tdz_last_error(void);
 /* Library version string. */
 const char *tdz_version(void);
 
+/* Number of device kernels this library has launched in this process. */
+long long tdz_launch_count(void);
+
 /* ---------------------------------------------------------------- space
  * Tensor B-spline space: per axis (x first) a clamped knot vector of
  * nknots[d] values and degree[d]; nquad Gauss-Legendre points per element
@@ -65,6 +68,12 @@ tdz_status tdz_space_ndof(const tdz_space *s, long long *ndof);
 /* Quadrature points and weights (times the element Jacobian) of one axis,
  * nel*nquad values each, element-major (PetIGA IGABasis point/weight*detJac). */
 tdz_status tdz_space_quadrature(const tdz_space *s, int axis, double *x, double *w);
+/* L2 load vector of one axis: out_i = sum_q w_q B_i(x_q) f(x_q) for complex
+ * values f at the quadrature points of the axis (interleaved re/im, nel*nquad
+ * of them); out has n complex entries (host arrays). With tdz_operator_mass_solve
+ * this is the M-projection of a separable initial state (the wave-packet
+ * projection of src/core.cpp:1187-1228, there by CG on the assembled M). */
+tdz_status tdz_space_project(const tdz_space *s, int axis, const double *f_q, double *out);
 void tdz_space_destroy(tdz_space *s);
 
 /* -------------------------------------------------------------- physics
@@ -110,6 +119,9 @@ tdz_status tdz_operator_set_stage(tdz_op *op, double alpha_re, double alpha_im, 
  * (src/propagator.cpp:622-623, src/monitor.cpp:114-116) and
  * TDSEZTensorOps::Apply (src/tensorops.cpp:155-188). x and y must not alias. */
 tdz_status tdz_operator_apply(tdz_op *op, int which, int precision, const void *x, void *y, void *stream);
+/* x <- M^-1 x in place (exact Kronecker inverse of the overlap, banded
+ * Cholesky line solves), FP32 or FP64 device vector. */
+tdz_status tdz_operator_mass_solve(tdz_op *op, int precision, void *x, void *stream);
 /* Number of fused-apply kernel launches issued so far by this operator. */
 long long tdz_operator_launches(const tdz_op *op);
 void tdz_operator_destroy(tdz_op *op);
@@ -143,7 +155,19 @@ tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stre
  * (PETSc KSPConvergedReason numbering: -3 iteration cap, -9 NaN/Inf). */
 tdz_status tdz_solver_solve(tdz_solver *s, const void *b, void *x, void *stream, int *its, int *reason,
                             double *rnorm);
+/* z = P^-1 r: one application of the solver's preconditioner (one V-cycle
+ * for TDZ_PC_MG) on FP64 device vectors; the PCShell PCApply of a PETSc
+ * adapter (the PCMG V-cycle of src/multigrid.cpp:275-325). */
+tdz_status tdz_solver_precondition(tdz_solver *s, const void *r, void *z, void *stream);
 void tdz_solver_destroy(tdz_solver *s);
+
+/* out = sum_i conj(x_i) y_i over n complex coefficients (FP32 or FP64 device
+ * vectors), accumulated in FP64 by a deterministic two-pass reduction (the
+ * VecDot of the Krylov and monitor paths, e.g. <psi|D|psi> after
+ * tdz_operator_apply). out: one complex double (16 bytes) in device memory.
+ * The per-block partial sums live in library-owned device scratch, allocated
+ * on the first call on each device. */
+tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision, void *out, void *stream);
 
 /* ----------------------------------------------------------- propagator
  * Time steps of TDSEZPropagator::Evolve (CN, src/propagator.cpp:78-251) and
@@ -167,6 +191,62 @@ tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, con
 tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies,
                           long long *cycles, int *last_its, double *last_rres);
 void tdz_prop_destroy(tdz_prop *p);
+
+/* --------------------------------------------------------------- t-SURFF
+ * Photoelectron amplitudes from the surface flux through the box |x_d| = R
+ * (TDSEZTSurff, include/tdsez_tsurff.hpp, src/tsurff.cpp:112-559): surface
+ * Gauss points of every knot span inside [-R, R], trace of psi and
+ * (1/m) d_n psi, Volkov integrals A' = -s E, B' = A, C' = |A|^2/2m + V0 by
+ * RK4 substeps of at most dt/2, flux on the momentum grid factorised by axis
+ * (FluxGrid), trapezoid accumulation over samples (AddFlux). Momenta are
+ * ordered k_x slowest, k_z fastest. The field callback returns the physical
+ * field E_a(t) (0 on uncoupled axes).
+ */
+typedef double (*tdz_field_fn)(int axis, double t, void *ctx);
+typedef struct tdz_tsurff tdz_tsurff;
+typedef struct tdz_tsurff_opts {
+    double radius;      /* SurffRadius R                                     */
+    int nquad;          /* Gauss points per span on the surface; 0 = space's */
+    int nk[3];          /* momentum grid points per axis (used axes)          */
+    double kmin[3], kmax[3];
+    double mass;        /* exterior mass                                     */
+    double v0;          /* exterior carrier potential s V (Ha)               */
+    double charge;      /* q; s = -q                                         */
+    double dt;          /* TimeStep                                          */
+} tdz_tsurff_opts;
+tdz_status tdz_tsurff_create(const tdz_space *s, const tdz_tsurff_opts *o, tdz_field_fn field, void *ctx,
+                             tdz_tsurff **out);
+/* Add the flux of psi (FP64 device vector) at time t (increasing). */
+tdz_status tdz_tsurff_sample(tdz_tsurff *ts, double t, const void *psi, void *stream);
+/* Accumulated amplitudes b(k), prod(nk) complex values (host array). */
+tdz_status tdz_tsurff_amplitudes(tdz_tsurff *ts, double *out, void *stream);
+/* Volkov integrals at the last sample: A[3], B[3], C, t (8 doubles). */
+tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct);
+void tdz_tsurff_destroy(tdz_tsurff *ts);
+
+/* ------------------------------------------------------ learned correction
+ * Small 3D convolutional network (3x3x3 convolutions, zero padding, ReLU
+ * between layers, BF16 weights, FP32 accumulation) with hand-written
+ * forward, backward and Adam kernels. It is trained on residual/error pairs
+ * that the solver generates and serves as a learned coarse correction inside
+ * the multigrid cycle (no counterpart in the reference, which has ASM/ILU
+ * and PCMG only). Tensors are FP32 device arrays [batch][channel][D][H][W].
+ */
+typedef struct tdz_cnn tdz_cnn;
+tdz_status tdz_cnn_create(int cin, int width, int cout, int layers, int D, int H, int W, int batch,
+                          unsigned long long seed, tdz_cnn **out);
+tdz_status tdz_cnn_forward(tdz_cnn *n, const float *in, float *out, int batch, void *stream);
+/* One Adam step on the relative MSE sum_b ||y_b - t_b||^2 / ||t_b||^2 / B. */
+tdz_status tdz_cnn_train_step(tdz_cnn *n, const float *in, const float *target, int batch, float lr, void *stream);
+/* Loss accumulated since the last call (resets it). */
+tdz_status tdz_cnn_loss(tdz_cnn *n, float *loss, void *stream);
+/* Number of parameters; get / set the FP32 master parameters (per layer:
+ * weights [co][ci][3][3][3], then bias [co]); gradients of the last step. */
+tdz_status tdz_cnn_num_params(const tdz_cnn *n, long long *count);
+tdz_status tdz_cnn_get_params(const tdz_cnn *n, float *host);
+tdz_status tdz_cnn_set_params(tdz_cnn *n, const float *host);
+tdz_status tdz_cnn_get_grads(const tdz_cnn *n, float *host);
+void tdz_cnn_destroy(tdz_cnn *n);
 
 #ifdef __cplusplus
 }

@@ -383,3 +383,38 @@ def kron_apply(space: Space, terms, x: np.ndarray) -> np.ndarray:
             T = band_apply_axis(t.bands[d], space.axes[d].p, T, dim - 1 - d)
         Y += t.coef * T
     return Y.reshape(-1)
+
+
+def band_sparse(A: np.ndarray, p: int):
+    """Sparse n x n matrix of a 1D band."""
+    n = A.shape[0]
+    rows, cols, vals = [], [], []
+    for k in range(-p, p + 1):
+        i = np.arange(max(0, -k), min(n, n - k))
+        rows.append(i)
+        cols.append(i + k)
+        vals.append(A[i, k + p])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+
+
+def kron_assemble(space: Space, terms):
+    """Assembled sum_t coef_t (A_z (x) A_y (x) A_x) as a scipy sparse matrix."""
+    out = None
+    for t in terms:
+        mats = [band_sparse(t.bands[d], space.axes[d].p) for d in range(space.dim)]
+        m = t.coef * _kron(mats)
+        out = m if out is None else out + m
+    return out.tocsr()
+
+
+def kron_operators(space: Space, phys: Physics):
+    """M, H (+CAP) and the coupled dipoles of a separable physics, assembled
+    from their Kronecker factors (equal to ``Assembled`` to rounding)."""
+    M = kron_assemble(space, [t for t in kron_terms(space, phys, g=0.0, alpha=1.0) if t.name == "M"])
+    H = kron_assemble(space, [t for t in kron_terms(space, phys, g=1.0, alpha=0.0) if t.name != "M"])
+    D = []
+    for a in phys.coupled:
+        c = [1.0 if b == a else 0.0 for b in phys.coupled]
+        D.append(kron_assemble(space, [t for t in kron_terms(space, phys, g=1.0, c=c, alpha=0.0)
+                                       if t.name == f"D{a}"]))
+    return M, H, D

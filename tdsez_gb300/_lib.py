@@ -52,6 +52,22 @@ class tdz_solver_opts(C.Structure):
     ]
 
 
+class tdz_tsurff_opts(C.Structure):
+    _fields_ = [
+        ("radius", C.c_double),
+        ("nquad", C.c_int),
+        ("nk", C.c_int * 3),
+        ("kmin", C.c_double * 3),
+        ("kmax", C.c_double * 3),
+        ("mass", C.c_double),
+        ("v0", C.c_double),
+        ("charge", C.c_double),
+        ("dt", C.c_double),
+    ]
+
+
+FIELD_FN = C.CFUNCTYPE(C.c_double, C.c_int, C.c_double, C.c_void_p)
+
 TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG = 0, 1, 2
 TDZ_CN, TDZ_PADE22, TDZ_MAGNUS4 = 0, 1, 2
 
@@ -67,24 +83,43 @@ LL = C.c_longlong
 SIGNATURES = {
     "tdz_last_error": (C.c_char_p, []),
     "tdz_version": (C.c_char_p, []),
+    "tdz_launch_count": (LL, []),
     "tdz_space_create": (I, [I, C.POINTER(I), C.POINTER(I), C.POINTER(C.POINTER(D)), I, PP]),
     "tdz_space_axis": (I, [VP, I, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
     "tdz_space_ndof": (I, [VP, C.POINTER(LL)]),
     "tdz_space_quadrature": (I, [VP, I, C.POINTER(D), C.POINTER(D)]),
+    "tdz_space_project": (I, [VP, I, C.POINTER(D), C.POINTER(D)]),
     "tdz_space_destroy": (None, [VP]),
     "tdz_operator_create": (I, [VP, C.POINTER(tdz_physics), PP]),
     "tdz_operator_set_stage": (I, [VP, D, D, D, D, I, C.POINTER(D)]),
     "tdz_operator_apply": (I, [VP, I, I, VP, VP, VP]),
+    "tdz_operator_mass_solve": (I, [VP, I, VP, VP]),
     "tdz_operator_launches": (LL, [VP]),
     "tdz_operator_destroy": (None, [VP]),
+    "tdz_vec_dot": (I, [VP, VP, LL, I, VP, VP]),
     "tdz_solver_create": (I, [VP, C.c_void_p, VP, PP]),
     "tdz_solver_solve": (I, [VP, VP, VP, VP, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
+    "tdz_solver_precondition": (I, [VP, VP, VP, VP]),
     "tdz_solver_destroy": (None, [VP]),
     "tdz_prop_create": (I, [VP, I, C.c_void_p, I, VP, PP]),
     "tdz_prop_step": (I, [VP, VP, D, C.POINTER(D), C.POINTER(D), VP]),
     "tdz_prop_stats": (I, [VP, C.POINTER(LL), C.POINTER(LL), C.POINTER(LL), C.POINTER(LL), C.POINTER(I),
                            C.POINTER(D)]),
     "tdz_prop_destroy": (None, [VP]),
+    "tdz_tsurff_create": (I, [VP, C.c_void_p, FIELD_FN, VP, PP]),
+    "tdz_tsurff_sample": (I, [VP, D, VP, VP]),
+    "tdz_tsurff_amplitudes": (I, [VP, C.POINTER(D), VP]),
+    "tdz_tsurff_volkov": (I, [VP, C.POINTER(D)]),
+    "tdz_tsurff_destroy": (None, [VP]),
+    "tdz_cnn_create": (I, [I, I, I, I, I, I, I, I, C.c_ulonglong, PP]),
+    "tdz_cnn_forward": (I, [VP, VP, VP, I, VP]),
+    "tdz_cnn_train_step": (I, [VP, VP, VP, I, C.c_float, VP]),
+    "tdz_cnn_loss": (I, [VP, C.POINTER(C.c_float), VP]),
+    "tdz_cnn_num_params": (I, [VP, C.POINTER(LL)]),
+    "tdz_cnn_get_params": (I, [VP, C.POINTER(C.c_float)]),
+    "tdz_cnn_set_params": (I, [VP, C.POINTER(C.c_float)]),
+    "tdz_cnn_get_grads": (I, [VP, C.POINTER(C.c_float)]),
+    "tdz_cnn_destroy": (None, [VP]),
 }
 
 

@@ -2,18 +2,24 @@
 // error of its body and returns a status code; the message is kept per thread
 // for tdz_last_error(). Mirrors the PetscErrorCode / PetscCall convention of
 // the reference (every call returns a code, no exception crosses the ABI).
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 
 #include "oper.h"
 #include "prop.h"
+#include "tsurff.h"
+#include "cnn.h"
 
 struct tdz_space {
     tdz::Space s;
 };
 struct tdz_op {
     tdz::Operator o;
+    std::unique_ptr<tdz::KronSolve> minv;
 };
 struct tdz_solver {
     tdz::Solver s;
@@ -21,10 +27,19 @@ struct tdz_solver {
 struct tdz_prop {
     tdz::Propagator p;
 };
+struct tdz_tsurff {
+    tdz::TSurff t;
+};
+struct tdz_cnn {
+    tdz::CNN n;
+};
 
 namespace tdz {
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+static std::atomic<long long> g_launches{0};
+void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace tdz
 
 template <class F> static tdz_status guarded(F &&f) {
@@ -49,6 +64,8 @@ extern "C" {
 const char *tdz_last_error(void) { return tdz::g_last_error.c_str(); }
 
 const char *tdz_version(void) { return "tdz 0.1 (sm_103a)"; }
+
+long long tdz_launch_count(void) { return tdz::launch_count(); }
 
 tdz_status tdz_space_create(int dim, const int *degree, const int *nknots, const double *const *knots, int nquad,
                             tdz_space **out) {
@@ -96,6 +113,23 @@ tdz_status tdz_space_quadrature(const tdz_space *s, int axis, double *x, double 
     });
 }
 
+tdz_status tdz_space_project(const tdz_space *s, int axis, const double *f_q, double *out) {
+    return guarded([&] {
+        TDZ_CHECK(s && f_q && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(axis >= 0 && axis < s->s.dim, TDZ_ERR_ARG, "axis out of range");
+        const tdz::Axis1D &a = s->s.ax[axis];
+        std::vector<tdz::cd> acc(a.n, 0.0);
+        const int np = a.p + 1;
+        for (int e = 0; e < a.nel; ++e)
+            for (int q = 0; q < a.nq; ++q) {
+                const size_t k = (size_t)e * a.nq + q;
+                const tdz::cd f(f_q[2 * k], f_q[2 * k + 1]);
+                for (int r = 0; r < np; ++r) acc[a.offset[e] + r] += a.wq[k] * a.N[k * np + r] * f;
+            }
+        for (int i = 0; i < a.n; ++i) { out[2 * i] = acc[i].real(); out[2 * i + 1] = acc[i].imag(); }
+    });
+}
+
 void tdz_space_destroy(tdz_space *s) { delete s; }
 
 tdz_status tdz_operator_create(const tdz_space *s, const tdz_physics *phys, tdz_op **out) {
@@ -126,9 +160,50 @@ tdz_status tdz_operator_apply(tdz_op *op, int which, int precision, const void *
     });
 }
 
+tdz_status tdz_operator_mass_solve(tdz_op *op, int precision, void *x, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(op && x, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
+        if (!op->minv) {
+            auto ks = std::make_unique<tdz::KronSolve>();
+            std::array<const tdz::BandD *, 3> mb{nullptr, nullptr, nullptr};
+            for (int d = 0; d < op->o.sp->dim; ++d) mb[d] = &op->o.bases[d][tdz::kM];
+            ks->setup(mb, op->o.sp->dim);
+            op->minv = std::move(ks);
+        }
+        op->minv->apply(x, precision, static_cast<cudaStream_t>(stream));
+        TDZ_CUDA(cudaGetLastError());
+    });
+}
+
 long long tdz_operator_launches(const tdz_op *op) { return op ? op->o.launches : 0; }
 
 void tdz_operator_destroy(tdz_op *op) { delete op; }
+
+namespace {
+// per-device reduction scratch of tdz_vec_dot (allocated on first use)
+std::mutex g_dot_mu;
+std::map<int, std::unique_ptr<tdz::blas::Reducer>> g_dot_scratch;
+}  // namespace
+
+tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision, void *out, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(x && y && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(n >= 0, TDZ_ERR_ARG, "negative length");
+        TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
+        int dev = 0;
+        TDZ_CUDA(cudaGetDevice(&dev));
+        tdz::blas::Reducer *r;
+        {
+            std::lock_guard<std::mutex> lk(g_dot_mu);
+            auto &slot = g_dot_scratch[dev];
+            if (!slot) slot = std::make_unique<tdz::blas::Reducer>();
+            r = slot.get();
+        }
+        tdz::blas::dot_device(*r, x, y, (size_t)n, precision, static_cast<double2 *>(out),
+                              static_cast<cudaStream_t>(stream));
+    });
+}
 
 static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     tdz::SolverOptions so;
@@ -166,6 +241,14 @@ tdz_status tdz_solver_solve(tdz_solver *s, const void *b, void *x, void *stream,
         if (its) *its = st.its;
         if (reason) *reason = st.reason;
         if (rnorm) *rnorm = st.rnorm;
+    });
+}
+
+tdz_status tdz_solver_precondition(tdz_solver *s, const void *r, void *z, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(s && r && z, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(r != z, TDZ_ERR_ARG, "r and z must not alias");
+        s->s.pc->apply(static_cast<const double2 *>(r), static_cast<double2 *>(z), static_cast<cudaStream_t>(stream));
     });
 }
 
@@ -224,5 +307,116 @@ tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, 
 }
 
 void tdz_prop_destroy(tdz_prop *p) { delete p; }
+
+tdz_status tdz_tsurff_create(const tdz_space *s, const tdz_tsurff_opts *o, tdz_field_fn field, void *ctx,
+                             tdz_tsurff **out) {
+    return guarded([&] {
+        TDZ_CHECK(s && o && out, TDZ_ERR_ARG, "null argument");
+        *out = nullptr;
+        auto h = std::make_unique<tdz_tsurff>();
+        h->t.setup(s->s, *o, field, ctx);
+        *out = h.release();
+    });
+}
+
+tdz_status tdz_tsurff_sample(tdz_tsurff *ts, double t, const void *psi, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(ts && psi, TDZ_ERR_ARG, "null argument");
+        ts->t.sample(t, static_cast<const double2 *>(psi), static_cast<cudaStream_t>(stream));
+    });
+}
+
+tdz_status tdz_tsurff_amplitudes(tdz_tsurff *ts, double *out, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(ts && out, TDZ_ERR_ARG, "null argument");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        TDZ_CUDA(cudaMemcpyAsync(out, ts->t.amp.ptr, ts->t.nktot * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        TDZ_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct) {
+    return guarded([&] {
+        TDZ_CHECK(ts && abct, TDZ_ERR_ARG, "null argument");
+        for (int d = 0; d < 3; ++d) { abct[d] = ts->t.A[d]; abct[3 + d] = ts->t.B[d]; }
+        abct[6] = ts->t.C;
+        abct[7] = ts->t.vt;
+    });
+}
+
+void tdz_tsurff_destroy(tdz_tsurff *ts) { delete ts; }
+
+tdz_status tdz_cnn_create(int cin, int width, int cout, int layers, int D, int H, int W, int batch,
+                          unsigned long long seed, tdz_cnn **out) {
+    return guarded([&] {
+        TDZ_CHECK(out, TDZ_ERR_ARG, "null argument");
+        *out = nullptr;
+        TDZ_CHECK(cin >= 1 && width >= 1 && cout >= 1 && layers >= 1 && D >= 1 && H >= 1 && W >= 1 && batch >= 1,
+                  TDZ_ERR_ARG, "bad network shape");
+        auto h = std::make_unique<tdz_cnn>();
+        h->n.init(cin, width, cout, layers, D, H, W, batch, seed);
+        *out = h.release();
+    });
+}
+
+tdz_status tdz_cnn_forward(tdz_cnn *n, const float *in, float *out, int batch, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(n && in && out, TDZ_ERR_ARG, "null argument");
+        n->n.forward(in, out, batch, static_cast<cudaStream_t>(stream), false);
+    });
+}
+
+tdz_status tdz_cnn_train_step(tdz_cnn *n, const float *in, const float *target, int batch, float lr, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(n && in && target, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(batch >= 1 && batch <= n->n.batch, TDZ_ERR_ARG, "bad batch");
+        n->n.train_step(in, target, batch, lr, static_cast<cudaStream_t>(stream));
+    });
+}
+
+tdz_status tdz_cnn_loss(tdz_cnn *n, float *loss, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(n && loss, TDZ_ERR_ARG, "null argument");
+        *loss = n->n.read_loss(static_cast<cudaStream_t>(stream));
+    });
+}
+
+tdz_status tdz_cnn_num_params(const tdz_cnn *n, long long *count) {
+    return guarded([&] {
+        TDZ_CHECK(n && count, TDZ_ERR_ARG, "null argument");
+        long long c = 0;
+        for (int l = 0; l < n->n.layers; ++l) c += (long long)n->n.co[l] * n->n.ci[l] * 27 + n->n.co[l];
+        *count = c;
+    });
+}
+
+tdz_status tdz_cnn_get_params(const tdz_cnn *n, float *host) {
+    return guarded([&] {
+        TDZ_CHECK(n && host, TDZ_ERR_ARG, "null argument");
+        std::vector<float> v;
+        n->n.get_params(v);
+        std::memcpy(host, v.data(), v.size() * sizeof(float));
+    });
+}
+
+tdz_status tdz_cnn_set_params(tdz_cnn *n, const float *host) {
+    return guarded([&] {
+        TDZ_CHECK(n && host, TDZ_ERR_ARG, "null argument");
+        long long c = 0;
+        for (int l = 0; l < n->n.layers; ++l) c += (long long)n->n.co[l] * n->n.ci[l] * 27 + n->n.co[l];
+        n->n.set_params(std::vector<float>(host, host + c));
+    });
+}
+
+tdz_status tdz_cnn_get_grads(const tdz_cnn *n, float *host) {
+    return guarded([&] {
+        TDZ_CHECK(n && host, TDZ_ERR_ARG, "null argument");
+        std::vector<float> v;
+        n->n.get_grads(v);
+        std::memcpy(host, v.data(), v.size() * sizeof(float));
+    });
+}
+
+void tdz_cnn_destroy(tdz_cnn *n) { delete n; }
 
 }  // extern "C"

@@ -82,6 +82,7 @@ void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, v
         }
     }
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace tdz

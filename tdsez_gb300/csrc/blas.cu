@@ -204,6 +204,7 @@ void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
     if (prec == TDZ_FP64) k_scale<double><<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), a.real(), a.imag(), n);
     else k_scale<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(x), a.real(), a.imag(), n);
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st) {
@@ -217,6 +218,7 @@ void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n,
                                                   static_cast<const float2 *>(x), b.real(), b.imag(),
                                                   static_cast<const float2 *>(z), c.real(), c.imag(), n);
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void axpby(void *y, cd a, const void *x, cd b, size_t n, int prec, cudaStream_t st) {
@@ -229,11 +231,13 @@ void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st) {
     if (px == TDZ_FP64) k_cast64to32<<<g, kThreads, 0, st>>>(static_cast<const double2 *>(x), static_cast<float2 *>(y), n);
     else k_cast32to64<<<g, kThreads, 0, st>>>(static_cast<const float2 *>(x), static_cast<double2 *>(y), n);
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
     k_add_cast<<<grid_for(n), kThreads, 0, st>>>(y, a.real(), a.imag(), x, n);
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void Reducer::init() {
@@ -258,10 +262,22 @@ void mdot(Reducer &r, const void *const *V, int k, const void *w, size_t n, int 
         else mdot_dispatch<float>(kk, pp, w, n, r.partial.as<double2>(), r.blocks, st);
         k_finish<<<kk, kThreads, 0, st>>>(r.partial.as<double2>(), r.blocks, r.result.as<double2>());
         TDZ_CUDA(cudaGetLastError());
+    count_launch();
         TDZ_CUDA(cudaMemcpyAsync(r.host, r.result.ptr, sizeof(double2) * kk, cudaMemcpyDeviceToHost, st));
         TDZ_CUDA(cudaStreamSynchronize(st));
         for (int i = 0; i < kk; ++i) out[c0 + i] = cd(r.host[i].x, r.host[i].y);
     }
+}
+
+void dot_device(Reducer &r, const void *x, const void *y, size_t n, int prec, double2 *out, cudaStream_t st) {
+    r.init();
+    PtrPack pp{};
+    pp.p[0] = x;
+    if (prec == TDZ_FP64) mdot_dispatch<double>(1, pp, y, n, r.partial.as<double2>(), r.blocks, st);
+    else mdot_dispatch<float>(1, pp, y, n, r.partial.as<double2>(), r.blocks, st);
+    k_finish<<<1, kThreads, 0, st>>>(r.partial.as<double2>(), r.blocks, out);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch(2);
 }
 
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st) {
@@ -277,6 +293,7 @@ void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec
         if (prec == TDZ_FP64) maxpy_dispatch<double>(kk, w, pp, cp, n, st);
         else maxpy_dispatch<float>(kk, w, pp, cp, n, st);
         TDZ_CUDA(cudaGetLastError());
+    count_launch();
     }
 }
 

@@ -38,6 +38,8 @@ struct Reducer {
 // out[i] = <V_i, w> = sum conj(V_i) w for i < k (any k; chunks of kMaxDot),
 // precision prec; results copied to the host (synchronises the stream).
 void mdot(Reducer &r, const void *const *V, int k, const void *w, size_t n, int prec, cd *out, cudaStream_t st);
+// out (device double2) = <x, y> with scratch partials r.partial (no host sync)
+void dot_device(Reducer &r, const void *x, const void *y, size_t n, int prec, double2 *out, cudaStream_t st);
 // w += sum_i a_i V_i
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st);
 // ||x||_2 (synchronises)

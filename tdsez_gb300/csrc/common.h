@@ -26,6 +26,10 @@ struct Error : std::runtime_error {
 
 void set_last_error(const std::string &msg);
 
+// Kernels launched by the library (all entry points), for launch accounting.
+void count_launch(long long n = 1);
+long long launch_count();
+
 #define TDZ_CHECK(cond, code, msg)                                                          \
     do {                                                                                    \
         if (!(cond)) throw ::tdz::Error((code), std::string(msg) + " (" __FILE__ ":" +      \

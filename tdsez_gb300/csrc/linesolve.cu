@@ -160,6 +160,7 @@ void run_axis(const T *L, int axis, typename CT<T>::type *x, int n0, int n1, int
         k_line_strided<T, P><<<grid, 128, 0, st>>>(L, n2, x, nl, 1, (size_t)n0 * n1, 0);
     }
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 template <class T>

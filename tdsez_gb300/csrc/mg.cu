@@ -60,6 +60,7 @@ void axis_contract(const RowSparse &A, int axis, const void *in, void *out, int 
                                                            static_cast<const float2 *>(in), static_cast<float2 *>(out),
                                                            o[0], o[1], o[2], n0, n1, accumulate);
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 }  // namespace tdz

@@ -290,6 +290,14 @@ void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, int steps, bool x
         op.apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
         blas::axpbypcz(m.r.ptr, 1.0, m.b.ptr, 0.0, m.t1.ptr, -1.0, n, prec, st);
     }
+    if (std::abs(delta) <= 1e-12 * std::abs(theta)) {
+        // degenerate segment: damped Richardson x += M^-1 r / theta
+        blas::copy(m.r.ptr, m.z.ptr, n, prec, st);
+        m.minv.apply(m.z.ptr, prec, st);
+        if (x_zero) blas::axpby(m.x.ptr, 1.0 / theta, m.z.ptr, 0.0, n, prec, st);
+        else blas::axpby(m.x.ptr, 1.0 / theta, m.z.ptr, 1.0, n, prec, st);
+        return;
+    }
     const cd sigma1 = theta / delta;
     cd rho = 1.0 / sigma1;
     blas::copy(m.r.ptr, m.z.ptr, n, prec, st);

@@ -138,6 +138,30 @@ class Operator:
                                                   C.c_void_p(y.data_ptr()), C.c_void_p(s)))
         return y
 
+    def mass_solve(self, x, stream=None):
+        """x <- M^-1 x in place (complex64 / complex128 CUDA tensor)."""
+        import torch
+        prec = _lib.TDZ_FP64 if x.dtype == torch.complex128 else _lib.TDZ_FP32
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _lib.check(_lib.load().tdz_operator_mass_solve(self.handle, prec, C.c_void_p(x.data_ptr()), C.c_void_p(s)))
+        return x
+
+    def separable_state(self, fns, device="cuda"):
+        """M-projection of prod_d f_d(x_d) onto the space (complex128 tensor),
+        normalised to psi^H M psi = 1."""
+        import torch
+        vecs = [torch.tensor(self.space.project(d, fns[d]), device=device) for d in range(self.space.dim)]
+        psi = vecs[-1]
+        for v in reversed(vecs[:-1]):
+            psi = torch.outer(psi, v).reshape(-1)
+        psi = psi.contiguous()
+        self.mass_solve(psi)
+        from . import _lib as L
+        m = torch.empty_like(psi)
+        self.apply(L.TDZ_MASS, psi, m)
+        psi /= torch.sqrt(torch.vdot(psi, m).real)
+        return psi
+
     @property
     def launches(self) -> int:
         return int(_lib.load().tdz_operator_launches(self.handle))

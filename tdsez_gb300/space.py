@@ -105,6 +105,14 @@ class Space:
         _lib.check(_lib.load().tdz_space_quadrature(self.handle, axis, _lib.dptr(x), _lib.dptr(w)))
         return x, w
 
+    def project(self, axis: int, f) -> np.ndarray:
+        """L2 load vector sum_q w_q B_i(x_q) f(x_q) of one axis (complex)."""
+        x, _ = self.quadrature(axis)
+        fq = np.ascontiguousarray(np.asarray(f(x), dtype=np.complex128).view(np.float64))
+        out = np.zeros(2 * self.n[axis])
+        _lib.check(_lib.load().tdz_space_project(self.handle, axis, _lib.dptr(fq), _lib.dptr(out)))
+        return out.view(np.complex128)
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value:

@@ -1,0 +1,65 @@
+"""Host side of the GPU t-SURFF sampler (mirrors TDSEZTSurff::Setup/Sample,
+``src/tsurff.cpp:112-469``): the flux is added on every OutputStrideSurff-th
+step and at FinalTime."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Sequence
+
+import numpy as np
+
+from . import _lib
+from .space import Space
+
+
+class TSurff:
+    def __init__(self, space: Space, radius: float, kgrid: Sequence[tuple], field: Callable[[float], Sequence[float]],
+                 dt: float, mass: float = 1.0, v0: float = 0.0, charge: float = -1.0, nquad: int = 0,
+                 stride: int = 1):
+        """kgrid: per axis (kmin, kmax, nk); field(t) -> E_a(t) for every axis."""
+        self.space = space
+        self.stride = stride
+        o = _lib.tdz_tsurff_opts()
+        o.radius = radius
+        o.nquad = nquad
+        for d in range(space.dim):
+            o.kmin[d], o.kmax[d], o.nk[d] = kgrid[d][0], kgrid[d][1], int(kgrid[d][2])
+        o.mass, o.v0, o.charge, o.dt = mass, v0, charge, dt
+        self.nk = [int(kgrid[d][2]) for d in range(space.dim)]
+
+        def cb(axis, t, ctx):
+            try:
+                e = field(t)
+                return float(e[axis]) if axis < len(e) else 0.0
+            except Exception:
+                return 0.0
+        self._cb = _lib.FIELD_FN(cb)
+        h = C.c_void_p()
+        _lib.check(_lib.load().tdz_tsurff_create(space.handle, C.byref(o), self._cb, None, C.byref(h)))
+        self.handle = h
+
+    def sample(self, t: float, psi, stream=None):
+        import torch
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _lib.check(_lib.load().tdz_tsurff_sample(self.handle, t, C.c_void_p(psi.data_ptr()), C.c_void_p(s)))
+
+    def amplitudes(self, stream=None) -> np.ndarray:
+        import torch
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        out = np.zeros(2 * int(np.prod(self.nk)))
+        _lib.check(_lib.load().tdz_tsurff_amplitudes(self.handle, _lib.dptr(out), C.c_void_p(s)))
+        return out.view(np.complex128)
+
+    def volkov(self):
+        out = np.zeros(8)
+        _lib.check(_lib.load().tdz_tsurff_volkov(self.handle, _lib.dptr(out)))
+        return out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().tdz_tsurff_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

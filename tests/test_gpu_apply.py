@@ -59,3 +59,27 @@ def test_stage_change_needs_no_rebuild(cuda):
         op.apply(_lib.TDZ_STAGE, xd, yd)
         ref = alpha * (A.M @ x) + g * (A.H_total() @ x + c0 * (A.D[2] @ x))
         assert _rel(yd.cpu().numpy(), ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_vec_dot(cuda):
+    """tdz_vec_dot (FP64 accumulation, deterministic) against numpy, FP32 and FP64."""
+    import ctypes as C
+    import torch
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(2)
+    n = 1_000_003
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = np.vdot(x, y)
+    out = torch.zeros(1, dtype=torch.complex128, device=cuda)
+    for dt, prec, tol in ((torch.complex128, _lib.TDZ_FP64, 1e-13), (torch.complex64, _lib.TDZ_FP32, 1e-6)):
+        xd, yd = torch.tensor(x, dtype=dt, device=cuda), torch.tensor(y, dtype=dt, device=cuda)
+        vals = []
+        for _ in range(2):
+            _lib.check(lib.tdz_vec_dot(C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), n, prec,
+                                       C.c_void_p(out.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+            vals.append(out.item())
+        assert vals[0] == vals[1]                      # bit-reproducible
+        assert abs(vals[0] - ref) <= tol * np.sqrt(n) * 2

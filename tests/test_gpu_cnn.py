@@ -1,0 +1,91 @@
+"""Learned coarse correction network: GPU forward and gradients of the
+hand-written kernels against the numpy oracle (oracle/cnn.py), and a short
+training run that lowers the loss."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import cnn as ocnn
+
+
+def bf16(a):
+    """Round float32 to bfloat16 (nearest even), returned as float64."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return u.view(np.float32).astype(np.float64)
+
+
+def _unpack(flat, shapes):
+    Ws, bs, o = [], [], 0
+    for co, ci in shapes:
+        n = co * ci * 27
+        Ws.append(flat[o:o + n].reshape(co, ci, 3, 3, 3))
+        o += n
+        bs.append(flat[o:o + co])
+        o += co
+    return Ws, bs
+
+
+@pytest.mark.gpu
+def test_cnn_gradients_match_oracle(cuda):
+    import torch
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    cin, width, cout, L, D, H, W, B = 4, 8, 2, 3, 5, 6, 7, 2
+    h = C.c_void_p()
+    _lib.check(lib.tdz_cnn_create(cin, width, cout, L, D, H, W, B, 7, C.byref(h)))
+    n = C.c_longlong()
+    _lib.check(lib.tdz_cnn_num_params(h, C.byref(n)))
+    rng = np.random.default_rng(1)
+    params = (0.2 * rng.standard_normal(n.value)).astype(np.float32)
+    _lib.check(lib.tdz_cnn_set_params(h, params.ctypes.data_as(C.POINTER(C.c_float))))
+    shapes = [(width, cin), (width, width), (cout, width)]
+    Ws, bs = _unpack(params.astype(np.float64), shapes)
+    Wq = [bf16(w) for w in Ws]          # the kernels multiply by BF16 weights
+    x = rng.standard_normal((B, cin, D, H, W)).astype(np.float32)
+    t = rng.standard_normal((B, cout, D, H, W)).astype(np.float32)
+    xd, td = torch.tensor(x, device=cuda), torch.tensor(t, device=cuda)
+    yd = torch.empty((B, cout, D, H, W), dtype=torch.float32, device=cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.check(lib.tdz_cnn_forward(h, C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), B, C.c_void_p(s)))
+    yref, _, _ = ocnn.forward(x.astype(np.float64), Wq, bs)
+    torch.cuda.synchronize()
+    assert np.abs(yd.cpu().numpy() - yref).max() <= 1e-4 * np.abs(yref).max()
+    # one step with lr = 0: gradients only
+    _lib.check(lib.tdz_cnn_train_step(h, C.c_void_p(xd.data_ptr()), C.c_void_p(td.data_ptr()), B, 0.0, C.c_void_p(s)))
+    loss = C.c_float()
+    _lib.check(lib.tdz_cnn_loss(h, C.byref(loss), C.c_void_p(s)))
+    g = np.zeros(n.value, dtype=np.float32)
+    _lib.check(lib.tdz_cnn_get_grads(h, g.ctypes.data_as(C.POINTER(C.c_float))))
+    Lref, gW, gb = ocnn.loss_and_grads(x.astype(np.float64), t.astype(np.float64), Wq, bs)
+    assert abs(loss.value - Lref) <= 1e-4 * Lref
+    gref = np.concatenate([np.concatenate([w.reshape(-1), b]) for w, b in zip(gW, gb)])
+    # data gradients pass through BF16 (flipped) weights: a few 1e-3 relative
+    assert np.linalg.norm(g - gref) <= 1e-2 * np.linalg.norm(gref)
+    lib.tdz_cnn_destroy(h)
+
+
+@pytest.mark.gpu
+def test_cnn_training_lowers_loss(cuda):
+    """Adam on a smoothing target (the network learns a fixed 3D stencil)."""
+    import torch
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    cin, width, cout, L, D, H, W, B = 2, 16, 2, 3, 8, 8, 8, 4
+    h = C.c_void_p()
+    _lib.check(lib.tdz_cnn_create(cin, width, cout, L, D, H, W, B, 3, C.byref(h)))
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    losses = []
+    for it in range(150):
+        x = torch.randn((B, cin, D, H, W), generator=g).to(cuda)
+        k = torch.ones((cin, 1, 3, 3, 3), device=cuda) / 27.0
+        t = torch.nn.functional.conv3d(x, k, padding=1, groups=cin)
+        _lib.check(lib.tdz_cnn_train_step(h, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), B, 3e-3, s))
+        if it % 10 == 9:
+            v = C.c_float()
+            _lib.check(lib.tdz_cnn_loss(h, C.byref(v), s))
+            losses.append(v.value / 10)
+    assert losses[-1] < 0.25 * losses[0], losses
+    lib.tdz_cnn_destroy(h)
