@@ -169,6 +169,14 @@ void tdz_solver_destroy(tdz_solver *s);
  * on the first call on each device. */
 tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision, void *out, void *stream);
 
+/* out[i] = sum_j conj(V_i[j]) w[j] for i < k (any k): the fused multi-dot of
+ * the classical Gram-Schmidt passes (VecMDot). V: host array of k device
+ * vector pointers; out: k complex doubles in device memory. Same reduction
+ * as tdz_vec_dot (library-owned scratch, allocated on first use per device;
+ * chunks of 16 vectors per pass). */
+tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n, int precision, void *out,
+                        void *stream);
+
 /* ----------------------------------------------------------- propagator
  * Time steps of TDSEZPropagator::Evolve (CN, src/propagator.cpp:78-251) and
  * EvolveRational / Pade22Step (src/propagator.cpp:564-769) on a device state

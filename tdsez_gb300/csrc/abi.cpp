@@ -3,6 +3,7 @@
 // for tdz_last_error(). Mirrors the PetscErrorCode / PetscCall convention of
 // the reference (every call returns a code, no exception crosses the ABI).
 #include <atomic>
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -202,6 +203,32 @@ tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision,
         }
         tdz::blas::dot_device(*r, x, y, (size_t)n, precision, static_cast<double2 *>(out),
                               static_cast<cudaStream_t>(stream));
+    });
+}
+
+tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n, int precision, void *out,
+                        void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(V && w && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(k >= 1 && n >= 0, TDZ_ERR_ARG, "bad sizes");
+        TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
+        for (int i = 0; i < k; ++i) TDZ_CHECK(V[i], TDZ_ERR_ARG, "null vector in V");
+        int dev = 0;
+        TDZ_CUDA(cudaGetDevice(&dev));
+        tdz::blas::Reducer *r;
+        {
+            std::lock_guard<std::mutex> lk(g_dot_mu);
+            auto &slot = g_dot_scratch[dev];
+            if (!slot) slot = std::make_unique<tdz::blas::Reducer>();
+            r = slot.get();
+        }
+        r->init();
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        double2 *o = static_cast<double2 *>(out);
+        for (int c0 = 0; c0 < k; c0 += tdz::blas::kMaxDot) {
+            const int kk = std::min(tdz::blas::kMaxDot, k - c0);
+            tdz::blas::mdot_partials(V + c0, kk, w, (size_t)n, precision, r->partial.as<double2>(), r->blocks, o + c0, st);
+        }
     });
 }
 

@@ -280,6 +280,18 @@ void dot_device(Reducer &r, const void *x, const void *y, size_t n, int prec, do
     count_launch(2);
 }
 
+void mdot_partials(const void *const *V, int k, const void *w, size_t n, int prec, double2 *partial, int blocks,
+                   double2 *out, cudaStream_t st) {
+    TDZ_CHECK(k >= 1 && k <= kMaxDot, TDZ_ERR_INTERNAL, "bad multi-dot width");
+    PtrPack pp{};
+    for (int i = 0; i < k; ++i) pp.p[i] = V[i];
+    if (prec == TDZ_FP64) mdot_dispatch<double>(k, pp, w, n, partial, blocks, st);
+    else mdot_dispatch<float>(k, pp, w, n, partial, blocks, st);
+    k_finish<<<k, kThreads, 0, st>>>(partial, blocks, out);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch(2);
+}
+
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st) {
     for (int c0 = 0; c0 < k; c0 += kMaxDot) {
         const int kk = std::min(kMaxDot, k - c0);

@@ -40,6 +40,11 @@ struct Reducer {
 void mdot(Reducer &r, const void *const *V, int k, const void *w, size_t n, int prec, cd *out, cudaStream_t st);
 // out (device double2) = <x, y> with scratch partials r.partial (no host sync)
 void dot_device(Reducer &r, const void *x, const void *y, size_t n, int prec, double2 *out, cudaStream_t st);
+// out[i] = <V_i, w> for i < k <= kMaxDot into device memory, per-block
+// partials in the given scratch (blocks * k double2), no host sync
+void mdot_partials(const void *const *V, int k, const void *w, size_t n, int prec, double2 *partial, int blocks,
+                   double2 *out, cudaStream_t st);
+constexpr int kRedBlocksPublic = 2 * 152;   // blocks of the reductions (partials per dot product)
 // w += sum_i a_i V_i
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st);
 // ||x||_2 (synchronises)

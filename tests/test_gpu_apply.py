@@ -83,3 +83,22 @@ def test_vec_dot(cuda):
             vals.append(out.item())
         assert vals[0] == vals[1]                      # bit-reproducible
         assert abs(vals[0] - ref) <= tol * np.sqrt(n) * 2
+
+
+@pytest.mark.gpu
+def test_vec_mdot(cuda):
+    """tdz_vec_mdot (k = 20 > one 16-vector pass) against numpy."""
+    import ctypes as C
+    import torch
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    n, k = 300_001, 20
+    V = [torch.tensor(rng.standard_normal(n) + 1j * rng.standard_normal(n), device=cuda) for _ in range(k)]
+    w = torch.tensor(rng.standard_normal(n) + 1j * rng.standard_normal(n), device=cuda)
+    out = torch.zeros(k, dtype=torch.complex128, device=cuda)
+    ptrs = (C.c_void_p * k)(*[v.data_ptr() for v in V])
+    _lib.check(lib.tdz_vec_mdot(ptrs, k, C.c_void_p(w.data_ptr()), n, _lib.TDZ_FP64, C.c_void_p(out.data_ptr()),
+                                C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    ref = np.array([np.vdot(v.cpu().numpy(), w.cpu().numpy()) for v in V])
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max() + 1e-9
