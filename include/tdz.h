@@ -177,6 +177,21 @@ tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision,
 tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n, int precision, void *out,
                         void *stream);
 
+/* Allocation-free tdz_vec_mdot, for callers that cannot allocate device memory
+ * (a host application that owns every device allocation, e.g. a PETSc build
+ * with a fixed device pool, or a time step that must not hit cudaMalloc's
+ * implicit synchronisation). No counterpart in the reference.
+ * The per-block partial sums live in a static device array of the library
+ * (8 x 304 complex doubles = 38 KB, held by every GPU that loads the library
+ * until the process exits); at most 8 dot products per call, larger k is
+ * rejected with TDZ_ERR_ARG. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams, or different host threads on one device) race. Calls no
+ * cudaMalloc / cudaFree and no allocating library routine. */
+tdz_status tdz_vec_mdot_noalloc(const void *const *V, int k, const void *w, long long n, int precision, void *out,
+                                void *stream);
+
 /* ----------------------------------------------------------- propagator
  * Time steps of TDSEZPropagator::Evolve (CN, src/propagator.cpp:78-251) and
  * EvolveRational / Pade22Step (src/propagator.cpp:564-769) on a device state

@@ -98,6 +98,7 @@ SIGNATURES = {
     "tdz_operator_destroy": (None, [VP]),
     "tdz_vec_dot": (I, [VP, VP, LL, I, VP, VP]),
     "tdz_vec_mdot": (I, [C.POINTER(VP), I, VP, LL, I, VP, VP]),
+    "tdz_vec_mdot_noalloc": (I, [C.POINTER(VP), I, VP, LL, I, VP, VP]),
     "tdz_solver_create": (I, [VP, C.c_void_p, VP, PP]),
     "tdz_solver_solve": (I, [VP, VP, VP, VP, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
     "tdz_solver_precondition": (I, [VP, VP, VP, VP]),

@@ -232,6 +232,17 @@ tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n,
     });
 }
 
+tdz_status tdz_vec_mdot_noalloc(const void *const *V, int k, const void *w, long long n, int precision, void *out,
+                                void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(V && w && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(n >= 0, TDZ_ERR_ARG, "negative length");
+        TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
+        for (int i = 0; i < k; ++i) TDZ_CHECK(V[i], TDZ_ERR_ARG, "null vector in V");
+        tdz::mdot_noalloc(V, k, w, (size_t)n, precision, static_cast<double2 *>(out), static_cast<cudaStream_t>(stream));
+    });
+}
+
 static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     tdz::SolverOptions so;
     if (!o) return so;

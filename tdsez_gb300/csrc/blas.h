@@ -51,4 +51,9 @@ void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec
 double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st);
 
 }  // namespace blas
+
+// tdz_vec_mdot with the partial sums in the library's static device array
+// (noalloc.cu): k <= 8, no device allocation.
+void mdot_noalloc(const void *const *V, int k, const void *w, size_t n, int prec, double2 *out, cudaStream_t st);
+
 }  // namespace tdz
