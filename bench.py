@@ -150,10 +150,12 @@ def run_tdz(args):
     dt = w.dt
     mg = dict(pc="mg", rtol=RTOL, mg_smooth=args.mg_smooth, mg_coarse_its=args.mg_coarse_its,
               mg_levels=args.mg_levels)
+    if args.apply_only:
+        return apply_only(args, op, S, psi0, stream)
 
-    # ---- mixed precision arm (headline)
+    # ---- headline arm: FP64 FGMRES, FP32 preconditioner (fast diagonalisation)
     t_setup = time.time()
-    G = Propagator(op, "cn", field=w.field, precision="fp32", **mg)
+    G = Propagator(op, "cn", field=w.field, precision="fp32", pc=args.pc, rtol=RTOL, outer=args.outer)
     t_setup = time.time() - t_setup
     psi = psi0.clone()
     t = 0.0
@@ -191,34 +193,37 @@ def run_tdz(args):
     y64 = torch.empty_like(psi)
     t32 = time_kernel(lambda: op.apply(L.TDZ_STAGE, x32, y32), 20, stream)
     t64 = time_kernel(lambda: op.apply(L.TDZ_STAGE, psi, y64), 10, stream)
+    tdf = time_kernel(lambda: op.apply(L.TDZ_STAGE, psi, y64, df=True), 10, stream)
     pk = peaks()
     bytes32 = 16.0 * N          # x read + y written, complex FP32
     bytes64 = 32.0 * N
     ach32 = bytes32 / t32 / 1e9
     ach64 = bytes64 / t64 / 1e9
 
-    # ---- plain GPU multigrid arm (FP64 throughout)
-    plain = None
-    if args.plain_steps > 0:
-        Gp = Propagator(op, "cn", field=w.field, precision="fp64", **mg)
+    def run_arm(precision, nsteps, **kw):
+        Gp = Propagator(op, "cn", field=w.field, precision=precision, **kw)
         pp = psi0.clone()
         tp = 0.0
-        Gp.step(pp, tp, dt)
-        tp += dt
+        for i in range(args.warmup):
+            Gp.step(pp, tp, dt)
+            tp += dt
         torch.cuda.synchronize()
         sp0 = Gp.stats()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for i in range(args.plain_steps):
+        for i in range(nsteps):
             Gp.step(pp, tp, dt)
             tp += dt
         e1.record(stream)
         torch.cuda.synchronize()
         tpl = e0.elapsed_time(e1) / 1e3
         sp1 = Gp.stats()
-        plain = {"steps_per_s": args.plain_steps / tpl, "its_per_step": (sp1["its"] - sp0["its"]) / args.plain_steps,
-                 "steps": args.plain_steps}
-        del Gp
+        return {"steps_per_s": nsteps / tpl, "its_per_step": (sp1["its"] - sp0["its"]) / nsteps, "steps": nsteps}
+
+    mixed_mg = run_arm("fp32", args.mg_steps, outer=args.outer, **mg) if args.mg_steps > 0 else None
+
+    # ---- plain GPU multigrid arm (FP64 throughout)
+    plain = run_arm("fp64", args.plain_steps, **mg) if args.plain_steps > 0 else None
 
     # ---- e2e through the C ABI with host buffers
     host = psi.cpu().pin_memory()
@@ -243,11 +248,13 @@ def run_tdz(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 FGMRES) + c64 (FP32 multigrid)",
         "data": "synthetic (seeded heterostructure, Gaussian packet)",
         "config": {"workload": "3D heterostructure CN, 160x160x320 el, p=3, 5 C0 interfaces, N=%d" % N,
-                   "global_batch": world, "dt": dt, "rtol": RTOL, "precond": "B-spline multigrid (FP32)",
+                   "global_batch": world, "dt": dt, "rtol": RTOL, "precond": args.pc + " (FP32) in FP64 FGMRES",
+                   "outer_apply": {"df": "double-float (FP32 pairs)", "fp64": "native FP64"}[args.outer],
                    "mg": {"smooth": args.mg_smooth, "coarse_its": args.mg_coarse_its, "levels": args.mg_levels},
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "working set > L2 (state alone 141.6 MB)"},
         "its_per_step": its_per_step,
+        "mixed_mg": mixed_mg,
         "plain_mg": plain,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
                 "steps": ke},
@@ -256,7 +263,9 @@ def run_tdz(args):
                      "achieved": ach32, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                      "frac": ach32 / pk.get("hbm_gbs", 6800.0), "traffic": None,
                      "launch_us": t32 * 1e6, "bytes_per_launch": bytes32,
-                     "fp64_apply": {"achieved": ach64, "launch_us": t64 * 1e6, "bytes_per_launch": bytes64}},
+                     "fp64_apply": {"achieved": ach64, "launch_us": t64 * 1e6, "bytes_per_launch": bytes64},
+                     "df_apply": {"achieved": bytes64 / tdf / 1e9, "launch_us": tdf * 1e6,
+                                  "bytes_per_launch": bytes64}},
         "clocks": clk.summary(),
         "setup_s": t_setup,
     }
@@ -270,6 +279,24 @@ def run_tdz(args):
 
 
 CPU_GRID = (16, 16, 32)
+
+
+def apply_only(args, op, S, psi0, stream):
+    """Time the fused stage apply alone (FP32 and FP64), args.steps launches
+    each after 3 warm-up launches: the command profiled for the kernel."""
+    import torch
+    from tdsez_gb300 import _lib as L
+    op.set_stage(1.0, 0.25j, [0.001])
+    x32 = psi0.to(torch.complex64)
+    y32 = torch.empty_like(x32)
+    y64 = torch.empty_like(psi0)
+    t32 = time_kernel(lambda: op.apply(L.TDZ_STAGE, x32, y32), args.steps, stream)
+    t64 = time_kernel(lambda: op.apply(L.TDZ_STAGE, psi0, y64), max(1, args.steps // 4), stream)
+    tdf = time_kernel(lambda: op.apply(L.TDZ_STAGE, psi0, y64, df=True), max(1, args.steps // 2), stream)
+    N = S.ndof
+    print(json.dumps({"apply_fp32_us": t32 * 1e6, "apply_fp32_gbs": 16.0 * N / t32 / 1e9,
+                      "apply_fp64_us": t64 * 1e6, "apply_fp64_gbs": 32.0 * N / t64 / 1e9,
+                      "apply_df_us": tdf * 1e6, "apply_df_gbs": 32.0 * N / tdf / 1e9, "N": N}))
 
 
 def cpu_baseline(n_full: int, dt: float, seconds: float):
@@ -306,8 +333,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tdz")
-    ap.add_argument("--plain-steps", type=int, default=2)
-    ap.add_argument("--mg-smooth", type=int, default=2)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--mg-steps", type=int, default=2)
+    ap.add_argument("--pc", default="fdm")
+    ap.add_argument("--outer", default="df", choices=["df", "fp64"])
+    ap.add_argument("--apply-only", action="store_true")
+    ap.add_argument("--mg-smooth", type=int, default=8)
     ap.add_argument("--mg-coarse-its", type=int, default=12)
     ap.add_argument("--mg-levels", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -12,7 +12,7 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "libtdz.so"
 
 TDZ_OK = 0
-TDZ_FP32, TDZ_FP64 = 0, 1
+TDZ_FP32, TDZ_FP64, TDZ_FP64_DF = 0, 1, 2
 TDZ_MASS, TDZ_HAMILTONIAN, TDZ_DIPOLE_X, TDZ_DIPOLE_Y, TDZ_DIPOLE_Z, TDZ_STAGE = range(6)
 
 STATUS_NAMES = {0: "TDZ_OK", 1: "TDZ_ERR_ARG", 2: "TDZ_ERR_CUDA", 3: "TDZ_ERR_NOT_CONVERGED",
@@ -49,6 +49,7 @@ class tdz_solver_opts(C.Structure):
         ("mg_levels", C.c_int),
         ("mg_smooth", C.c_int),
         ("mg_coarse_its", C.c_int),
+        ("outer_precision", C.c_int),
     ]
 
 
@@ -68,7 +69,7 @@ class tdz_tsurff_opts(C.Structure):
 
 FIELD_FN = C.CFUNCTYPE(C.c_double, C.c_int, C.c_double, C.c_void_p)
 
-TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG = 0, 1, 2
+TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG, TDZ_PC_FDM = 0, 1, 2, 3
 TDZ_CN, TDZ_PADE22, TDZ_MAGNUS4 = 0, 1, 2
 
 _lib = None

@@ -41,7 +41,7 @@ def _flags(src: Path):
 
 def _digest() -> str:
     h = hashlib.sha256()
-    for p in sources() + sorted(CSRC.glob("*.h")) + [HERE.parent / "include" / "tdz.h"]:
+    for p in sources() + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "tdz.h"]:
         h.update(p.name.encode())
         h.update(p.read_bytes())
     h.update(" ".join(ARCH).encode())

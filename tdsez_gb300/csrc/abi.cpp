@@ -253,8 +253,11 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     so.pc_precision = o->pc_precision;
     TDZ_CHECK(so.pc_precision == TDZ_FP32 || so.pc_precision == TDZ_FP64, TDZ_ERR_ARG, "bad pc_precision");
     so.mg.levels = o->mg_levels;
-    so.mg.smooth = o->mg_smooth > 0 ? o->mg_smooth : 2;
+    so.mg.smooth = o->mg_smooth > 0 ? o->mg_smooth : 8;
     so.mg.coarse_its = o->mg_coarse_its > 0 ? o->mg_coarse_its : 12;
+    so.outer = o->outer_precision == 0 ? TDZ_FP64 : o->outer_precision;
+    TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
+              "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;
 }
 

@@ -8,6 +8,9 @@ namespace tdz {
 
 namespace {
 
+template <class T> T to_t(double v) { return (T)v; }
+template <> dff to_t<dff>(double v) { return dff_from(v); }
+
 template <class T>
 CombP<T> eval_comb(const Comb &c, const std::array<cd, 5> &sg) {
     CombP<T> out{};
@@ -15,25 +18,30 @@ CombP<T> eval_comb(const Comb &c, const std::array<cd, 5> &sg) {
     for (int i = 0; i < c.n; ++i) {
         const cd v = c.factor[i] * sg[c.scalar[i]];
         out.base[i] = c.base[i];
-        out.re[i] = (T)v.real();
-        out.im[i] = (T)v.imag();
+        out.re[i] = to_t<T>(v.real());
+        out.im[i] = to_t<T>(v.imag());
     }
     return out;
+}
+
+template <class T> const DevBuf &bands_of(const Operator &op, int d) {
+    if (std::is_same<T, double>::value) return op.dev64[d];
+    if (std::is_same<T, dff>::value) return op.devdf[d];
+    return op.dev32[d];
 }
 
 template <class T>
 ApplyParams<T> make_params(const Operator &op, const Plan &pl, const void *x, void *y) {
     ApplyParams<T> prm{};
     const Space &s = *op.sp;
-    const bool dbl = std::is_same<T, double>::value;
     prm.x = x;
     prm.y = y;
     prm.n0 = s.ax[0].n;
     prm.n1 = s.dim > 1 ? s.ax[1].n : 1;
     prm.n2 = s.dim > 2 ? s.ax[2].n : 1;
-    prm.b0 = static_cast<const T *>((dbl ? op.dev64[0] : op.dev32[0]).ptr);
-    prm.b1 = s.dim > 1 ? static_cast<const T *>((dbl ? op.dev64[1] : op.dev32[1]).ptr) : nullptr;
-    prm.b2 = s.dim > 2 ? static_cast<const T *>((dbl ? op.dev64[2] : op.dev32[2]).ptr) : nullptr;
+    prm.b0 = static_cast<const T *>(bands_of<T>(op, 0).ptr);
+    prm.b1 = s.dim > 1 ? static_cast<const T *>(bands_of<T>(op, 1).ptr) : nullptr;
+    prm.b2 = s.dim > 2 ? static_cast<const T *>(bands_of<T>(op, 2).ptr) : nullptr;
     const std::array<cd, 5> sg = op.sigma_for(pl.which);
     prm.xT = eval_comb<T>(pl.xT, sg);
     prm.yT = eval_comb<T>(pl.yT, sg);
@@ -47,8 +55,8 @@ ApplyParams<T> make_params(const Operator &op, const Plan &pl, const void *x, vo
             cd d = 0;
             if (pl.wall_m >= 0) d += sg[pl.wall_m] * op.m_wall[w];
             if (pl.wall_h >= 0) d += sg[pl.wall_h] * op.h_wall[w];
-            prm.wall_re[w] = (T)d.real();
-            prm.wall_im[w] = (T)d.imag();
+            prm.wall_re[w] = to_t<T>(d.real());
+            prm.wall_im[w] = to_t<T>(d.imag());
         }
     }
     return prm;
@@ -63,21 +71,23 @@ void launch_1d(const ApplyParams<T> &prm, cudaStream_t st) {
 }  // namespace
 
 void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st) {
-    const bool dbl = prec == TDZ_FP64;
     const int dim = op.sp->dim;
     if (dim == 1) {
-        if (dbl) launch_1d(make_params<double>(op, pl, x, y), st);
+        // 1D operators are tiny: the double-float request runs in native FP64
+        if (prec != TDZ_FP32) launch_1d(make_params<double>(op, pl, x, y), st);
         else launch_1d(make_params<float>(op, pl, x, y), st);
     } else {
         ApplyParams<float> pf{};
         ApplyParams<double> pd{};
-        if (dbl) pd = make_params<double>(op, pl, x, y);
+        ApplyParams<dff> pdf{};
+        if (prec == TDZ_FP64) pd = make_params<double>(op, pl, x, y);
+        else if (prec == TDZ_FP64_DF) pdf = make_params<dff>(op, pl, x, y);
         else pf = make_params<float>(op, pl, x, y);
         switch (op.P) {
-        case 2: apply_p2(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
-        case 3: apply_p3(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
-        case 4: apply_p4(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
-        case 5: apply_p5(dim, pl.hasB, pl.hasC, pf, pd, dbl, st); break;
+        case 2: apply_p2(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;
+        case 3: apply_p3(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;
+        case 4: apply_p4(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;
+        case 5: apply_p5(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;
         default: throw Error(TDZ_ERR_UNSUPPORTED, "2D/3D apply supports degrees 2..5");
         }
     }

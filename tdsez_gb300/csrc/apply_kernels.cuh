@@ -39,6 +39,7 @@ template <class T> struct ApplyParams {
     const T *b0, *b1, *b2;      // base bands per axis [nbase][n][2p+1]
     CombP<T> xT, yT, zA, zC;
     int zchunk;
+    int zchunk_planes;          // zchunk + 2p (rows of the precomputed outer bands)
     int p;                      // degree (1D kernel)
     T wall_re[2], wall_im[2];   // 1D walls: diagonal values, wall = 0 / n-1
     int walls;
@@ -50,26 +51,38 @@ __device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, 
     C z = czero<C>();
     for (int t = 0; t < cb.n; ++t) {
         const T b = bands[((size_t)cb.base[t] * n + i) * bw + o];
-        z.x = fma(cb.re[t], b, z.x);
-        z.y = fma(cb.im[t], b, z.y);
+        z.x = tfma(cb.re[t], b, z.x);
+        z.y = tfma(cb.im[t], b, z.y);
     }
     return z;
 }
 
 // ---------------------------------------------------------------- 3D kernel
+// Per z plane: (1) the prefetched input tile goes to shared memory, (2) barrier,
+// (3) the next plane's tile is requested into registers (its latency overlaps
+// the compute), (4) x stage into sU[buf], (5) barrier, (6) y stage and the
+// outer-stage ring update from sU[buf] and the precomputed band rows. sU is
+// double-buffered, so two barriers per plane suffice.
+constexpr int kLoadsPerThread3 = 4;   // covers (TY+2p)(TX+2p) / (TX TY) for p <= 5
+
 template <class T, int P, bool HB, bool HC, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     using C = typename CT<T>::type;
     constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
     constexpr int NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
     constexpr int UT = 1, US = HB ? 2 : 1;    // slots of u_T and u_S in sU
+    constexpr int NT = TX * TY;
+    static_assert(RY * RX <= kLoadsPerThread3 * NT, "tile larger than the prefetch registers");
     __shared__ C sIn[RY][RX];
-    __shared__ C sU[NU][RY][TX];
+    __shared__ C sU[2][NU][RY][TX];
     __shared__ T sYm[BW][TY];
     __shared__ T sYs[HC ? BW : 1][TY];
     __shared__ C sYt[HB ? BW : 1][TY];
-    __shared__ C sZA[BW], sZC[BW];
-    __shared__ T sZM[BW];
+    extern __shared__ unsigned char dyn_raw[];
+    // precomputed outer-band rows of the chunk: [plane][o] (A, C complex; M real)
+    C *sZA = reinterpret_cast<C *>(dyn_raw);
+    C *sZC = sZA + (size_t)prm.zchunk_planes * BW;
+    T *sZM = reinterpret_cast<T *>(sZC + (HC ? (size_t)prm.zchunk_planes * BW : 0));
 
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
     const int n0 = prm.n0, n1 = prm.n1, n2 = prm.n2;
@@ -79,8 +92,11 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     const int z0 = blockIdx.y * prm.zchunk;
     const int z1 = min(n2, z0 + prm.zchunk);
     if (z0 >= z1) return;
-    const C *__restrict__ X = static_cast<const C *>(prm.x);
-    C *__restrict__ Y = static_cast<C *>(prm.y);
+    using MC = typename MemC<T>::type;
+    const MC *__restrict__ X = static_cast<const MC *>(prm.x);
+    MC *__restrict__ Y = static_cast<MC *>(prm.y);
+    const int zs = z0 - P;
+    const int nplanes = (z1 - z0) + 2 * P;
 
     // band rows of this thread's x column
     T xm[BW], xs[HC ? BW : 1];
@@ -92,20 +108,43 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
         if constexpr (HC) xs[j] = in ? prm.b0[((size_t)kS * n0 + gx) * BW + j] : T(0);
         if constexpr (HB) xt[j] = in ? comb_at<T, C>(prm.xT, prm.b0, n0, BW, gx, j) : czero<C>();
     }
-    for (int i = tid; i < BW * TY; i += TX * TY) {
+    for (int i = tid; i < BW * TY; i += NT) {
         const int j = i / TY, r = i % TY, yy = y0 + r;
         const bool in = yy < n1;
         sYm[j][r] = in ? prm.b1[((size_t)kM * n1 + yy) * BW + j] : T(0);
         if constexpr (HC) sYs[j][r] = in ? prm.b1[((size_t)kS * n1 + yy) * BW + j] : T(0);
         if constexpr (HB) sYt[j][r] = in ? comb_at<T, C>(prm.yT, prm.b1, n1, BW, yy, j) : czero<C>();
     }
+    for (int i = tid; i < nplanes * BW; i += NT) {
+        const int pl = i / BW, o = i % BW, zin = zs + pl;
+        const bool in = zin >= 0 && zin < n2;
+        sZA[i] = in ? comb_at<T, C>(prm.zA, prm.b2, n2, BW, zin, o) : czero<C>();
+        if constexpr (HC) sZC[i] = in ? comb_at<T, C>(prm.zC, prm.b2, n2, BW, zin, o) : czero<C>();
+        if constexpr (HB) sZM[i] = in ? prm.b2[((size_t)kM * n2 + zin) * BW + o] : T(0);
+    }
+
+    // prefetch registers: element e = tid + q NT of the (RY x RX) tile
+    C pre[kLoadsPerThread3];
+    auto load_plane = [&](int zin) {
+#pragma unroll
+        for (int q = 0; q < kLoadsPerThread3; ++q) {
+            const int e = tid + q * NT;
+            C v = czero<C>();
+            if (e < RY * RX) {
+                const int r = e / RX, c = e % RX;
+                const int yy = y0 - P + r, xx = x0 - P + c;
+                if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) v = load_c<C>(X[((size_t)zin * n1 + yy) * n0 + xx]);
+            }
+            pre[q] = v;
+        }
+    };
+    const int zfirst = max(zs, 0);
+    load_plane(zfirst);
 
     C acc[BW];
 #pragma unroll
     for (int s = 0; s < BW; ++s) acc[s] = czero<C>();
 
-    const int zs = z0 - P;
-    const int nplanes = (z1 - z0) + 2 * P;
     for (int base = 0; base < nplanes; base += BW) {
 #pragma unroll
         for (int ph = 0; ph < BW; ++ph) {
@@ -113,20 +152,14 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
             if (it >= nplanes) break;
             const int zin = zs + it;
             if (zin >= 0 && zin < n2) {
-                __syncthreads();
-                for (int i = tid; i < RY * RX; i += TX * TY) {
-                    const int r = i / RX, c = i % RX;
-                    const int yy = y0 - P + r, xx = x0 - P + c;
-                    C v = czero<C>();
-                    if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) v = X[((size_t)zin * n1 + yy) * n0 + xx];
-                    sIn[r][c] = v;
-                }
-                if (tid < BW) {
-                    sZA[tid] = comb_at<T, C>(prm.zA, prm.b2, n2, BW, zin, tid);
-                    if constexpr (HB) sZM[tid] = prm.b2[((size_t)kM * n2 + zin) * BW + tid];
-                    if constexpr (HC) sZC[tid] = comb_at<T, C>(prm.zC, prm.b2, n2, BW, zin, tid);
+                const int buf = it & 1;
+#pragma unroll
+                for (int q = 0; q < kLoadsPerThread3; ++q) {
+                    const int e = tid + q * NT;
+                    if (e < RY * RX) sIn[e / RX][e % RX] = pre[q];
                 }
                 __syncthreads();
+                if (zin + 1 < n2 && zin + 1 < z1 + P) load_plane(zin + 1);
                 // x stage
                 for (int r = ty; r < RY; r += TY) {
                     C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
@@ -137,9 +170,9 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
                         if constexpr (HB) cfma(uT, xt[j], v);
                         if constexpr (HC) rfma(uS, xs[j], v);
                     }
-                    sU[0][r][tx] = uM;
-                    if constexpr (HB) sU[UT][r][tx] = uT;
-                    if constexpr (HC) sU[US][r][tx] = uS;
+                    sU[buf][0][r][tx] = uM;
+                    if constexpr (HB) sU[buf][UT][r][tx] = uT;
+                    if constexpr (HC) sU[buf][US][r][tx] = uS;
                 }
                 __syncthreads();
                 // y stage
@@ -147,29 +180,30 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
 #pragma unroll
                 for (int j = 0; j < BW; ++j) {
                     const T ym = sYm[j][ty];
-                    const C um = sU[0][ty + j][tx];
+                    const C um = sU[buf][0][ty + j][tx];
                     rfma(wA, ym, um);
                     if constexpr (HB) {
-                        rfma(wB, ym, sU[UT][ty + j][tx]);
+                        rfma(wB, ym, sU[buf][UT][ty + j][tx]);
                         cfma(wB, sYt[j][ty], um);
                     }
                     if constexpr (HC) {
-                        rfma(wC, ym, sU[US][ty + j][tx]);
+                        rfma(wC, ym, sU[buf][US][ty + j][tx]);
                         rfma(wC, sYs[j][ty], um);
                     }
                 }
                 // outer (z) stage
+                const C *zA = sZA + (size_t)it * BW;
 #pragma unroll
                 for (int o = 0; o < BW; ++o) {
                     C &a = acc[(ph - P + o + 2 * BW) % BW];
-                    cfma(a, sZA[o], wA);
-                    if constexpr (HB) rfma(a, sZM[o], wB);
-                    if constexpr (HC) cfma(a, sZC[o], wC);
+                    cfma(a, zA[o], wA);
+                    if constexpr (HB) rfma(a, sZM[(size_t)it * BW + o], wB);
+                    if constexpr (HC) cfma(a, sZC[(size_t)it * BW + o], wC);
                 }
             }
             if (it >= 2 * P) {
                 const int m = zin - P;
-                if (gx < n0 && gy < n1) Y[((size_t)m * n1 + gy) * n0 + gx] = acc[(ph - P + 2 * BW) % BW];
+                if (gx < n0 && gy < n1) Y[((size_t)m * n1 + gy) * n0 + gx] = store_c<MC>(acc[(ph - P + 2 * BW) % BW]);
             }
             acc[(ph - P + 2 * BW) % BW] = czero<C>();
         }
@@ -191,8 +225,9 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
     const int z0 = blockIdx.y * prm.zchunk;
     const int z1 = min(n1, z0 + prm.zchunk);
     if (z0 >= z1) return;
-    const C *__restrict__ X = static_cast<const C *>(prm.x);
-    C *__restrict__ Y = static_cast<C *>(prm.y);
+    using MC = typename MemC<T>::type;
+    const MC *__restrict__ X = static_cast<const MC *>(prm.x);
+    MC *__restrict__ Y = static_cast<MC *>(prm.y);
     T xm[BW], xs[HC ? BW : 1];
     C xt[HB ? BW : 1];
 #pragma unroll
@@ -217,7 +252,7 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
                 __syncthreads();
                 for (int c = tx; c < RX; c += TX) {
                     const int xx = x0 - P + c;
-                    sIn[c] = (xx >= 0 && xx < n0) ? X[(size_t)zin * n0 + xx] : czero<C>();
+                    sIn[c] = (xx >= 0 && xx < n0) ? load_c<C>(X[(size_t)zin * n0 + xx]) : czero<C>();
                 }
                 if (tx < BW) {
                     sZA[tx] = comb_at<T, C>(prm.zA, prm.b1, n1, BW, zin, tx);
@@ -243,7 +278,7 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
             }
             if (it >= 2 * P) {
                 const int m = zin - P;
-                if (gx < n0) Y[(size_t)m * n0 + gx] = acc[(ph - P + 2 * BW) % BW];
+                if (gx < n0) Y[(size_t)m * n0 + gx] = store_c<MC>(acc[(ph - P + 2 * BW) % BW]);
             }
             acc[(ph - P + 2 * BW) % BW] = czero<C>();
         }
@@ -291,11 +326,17 @@ inline int pick_chunk(int tiles, int n_outer, int P) {
 
 template <class T, int P, bool HB, bool HC>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
+    using C = typename CT<T>::type;
     ApplyParams<T> prm = prm0;
     const int tiles = ((prm.n0 + kTX3 - 1) / kTX3) * ((prm.n1 + kTY3 - 1) / kTY3);
-    prm.zchunk = pick_chunk(tiles, prm.n2, P);
+    prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P), 96);
+    prm.zchunk_planes = prm.zchunk + 2 * P;
+    const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
+    const size_t smem = rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
+    auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
+    if (smem > 48 * 1024) TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
-    k_apply3d<T, P, HB, HC, kTX3, kTY3><<<grid, dim3(kTX3, kTY3), 0, st>>>(prm);
+    kern<<<grid, dim3(kTX3, kTY3), smem, st>>>(prm);
 }
 
 template <class T, int P, bool HB, bool HC>
@@ -325,7 +366,7 @@ inline void dispatch_streams(int dim, bool hb, bool hc, const ApplyParams<T> &pr
 // per-degree entry points (apply_p<P>.cu)
 #define TDZ_APPLY_DECL(P)                                                                                  \
     void apply_p##P(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd, \
-                    bool dbl, cudaStream_t st);
+                    const ApplyParams<dff> &pdf, int prec, cudaStream_t st);
 TDZ_APPLY_DECL(2)
 TDZ_APPLY_DECL(3)
 TDZ_APPLY_DECL(4)

@@ -3,9 +3,10 @@
 
 namespace tdz {
 
-void apply_p3(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd, bool dbl,
-              cudaStream_t st) {
-    if (dbl) dispatch_streams<double, 3>(dim, hb, hc, pd, st);
+void apply_p3(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd,
+              const ApplyParams<dff> &pdf, int prec, cudaStream_t st) {
+    if (prec == TDZ_FP64) dispatch_streams<double, 3>(dim, hb, hc, pd, st);
+    else if (prec == TDZ_FP64_DF) dispatch_streams<dff, 3>(dim, hb, hc, pdf, st);
     else dispatch_streams<float, 3>(dim, hb, hc, pf, st);
 }
 

@@ -5,6 +5,8 @@
 #include "blas.h"
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 
 #include "cplx.cuh"
 
@@ -313,6 +315,7 @@ double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st) {
     cd v;
     const void *V[1] = {x};
     mdot(r, V, 1, x, n, prec, &v, st);
+    if (!std::isfinite(v.real())) return std::numeric_limits<double>::quiet_NaN();
     return std::sqrt(std::max(0.0, v.real()));
 }
 

@@ -1,0 +1,417 @@
+// Fast-diagonalisation preconditioner (Lynch-Rice-Thomas) for the z-layered
+// operator family: dense eigenvector transforms along x and y (smem-tiled
+// FP32 GEMMs) and one banded complex LU solve per (x, y) line along z with the
+// live stage coefficients. Exact inverse (up to FP32 rounding) when the inner
+// axes carry only mass and stiffness, which is the heterostructure's case.
+#include "fdm.h"
+
+#include <cmath>
+
+#include "apply_kernels.cuh"
+
+namespace tdz {
+
+// ---------------------------------------------------------------- host eigen
+void gen_eig(const BandD &S, const BandD &M, std::vector<double> &V, std::vector<double> &lam) {
+    const int n = S.n, p = S.p;
+    std::vector<double> L((size_t)n * n, 0.0), C((size_t)n * n, 0.0);
+    auto m = [&](int i, int j) { return std::abs(i - j) <= p ? M.at(i, j) : 0.0; };
+    auto s = [&](int i, int j) { return std::abs(i - j) <= p ? S.at(i, j) : 0.0; };
+    // Cholesky M = L L^T (banded)
+    for (int i = 0; i < n; ++i)
+        for (int j = std::max(0, i - p); j <= i; ++j) {
+            double v = m(i, j);
+            for (int k = std::max(0, i - p); k < j; ++k) v -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
+            if (i == j) {
+                TDZ_CHECK(v > 0, TDZ_ERR_INTERNAL, "mass band not positive definite");
+                L[(size_t)i * n + i] = std::sqrt(v);
+            } else L[(size_t)i * n + j] = v / L[(size_t)j * n + j];
+        }
+    // C = L^-1 S L^-T : first W = L^-1 S (columns), then C = W L^-T
+    std::vector<double> W((size_t)n * n, 0.0);
+    for (int c = 0; c < n; ++c)
+        for (int i = 0; i < n; ++i) {
+            double v = s(i, c);
+            for (int k = std::max(0, i - p); k < i; ++k) v -= L[(size_t)i * n + k] * W[(size_t)k * n + c];
+            W[(size_t)i * n + c] = v / L[(size_t)i * n + i];
+        }
+    for (int r = 0; r < n; ++r)
+        for (int i = 0; i < n; ++i) {
+            double v = W[(size_t)r * n + i];
+            for (int k = std::max(0, i - p); k < i; ++k) v -= L[(size_t)i * n + k] * C[(size_t)r * n + k];
+            C[(size_t)r * n + i] = v / L[(size_t)i * n + i];
+        }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j) {
+            const double a = 0.5 * (C[(size_t)i * n + j] + C[(size_t)j * n + i]);
+            C[(size_t)i * n + j] = C[(size_t)j * n + i] = a;
+        }
+    // cyclic Jacobi on C, accumulate Q
+    std::vector<double> Q((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                const double v = C[(size_t)i * n + j] * C[(size_t)i * n + j];
+                tot += v;
+                if (i != j) off += v;
+            }
+        if (off <= 1e-30 * tot) break;
+        for (int pi = 0; pi < n - 1; ++pi)
+            for (int qi = pi + 1; qi < n; ++qi) {
+                const double apq = C[(size_t)pi * n + qi];
+                if (std::abs(apq) < 1e-300) continue;
+                const double app = C[(size_t)pi * n + pi], aqq = C[(size_t)qi * n + qi];
+                const double theta = 0.5 * (aqq - app) / apq;
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::abs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = C[(size_t)k * n + pi], akq = C[(size_t)k * n + qi];
+                    C[(size_t)k * n + pi] = c * akp - sn * akq;
+                    C[(size_t)k * n + qi] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = C[(size_t)pi * n + k], aqk = C[(size_t)qi * n + k];
+                    C[(size_t)pi * n + k] = c * apk - sn * aqk;
+                    C[(size_t)qi * n + k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double qkp = Q[(size_t)k * n + pi], qkq = Q[(size_t)k * n + qi];
+                    Q[(size_t)k * n + pi] = c * qkp - sn * qkq;
+                    Q[(size_t)k * n + qi] = sn * qkp + c * qkq;
+                }
+            }
+    }
+    lam.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) lam[i] = C[(size_t)i * n + i];
+    // V = L^-T Q (back substitution with L^T, column by column)
+    V.assign((size_t)n * n, 0.0);
+    for (int c = 0; c < n; ++c)
+        for (int i = n - 1; i >= 0; --i) {
+            double v = Q[(size_t)i * n + c];
+            for (int k = i + 1; k <= std::min(n - 1, i + p); ++k) v -= L[(size_t)k * n + i] * V[(size_t)k * n + c];
+            V[(size_t)i * n + c] = v / L[(size_t)i * n + i];
+        }
+}
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+// C[M][N] (complex) = A[M][K] (complex, lda = K) . B[K][N] (real, ldb = N)
+__global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, const float *__restrict__ B,
+                                                 float2 *__restrict__ Cm, int M, int N, int K) {
+    __shared__ float2 As[BK][BM + 1];
+    __shared__ float Bs[BK][BN + 4];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    float2 acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        for (int i = threadIdx.x; i < BM * BK; i += 256) {
+            const int r = i / BK, k = i % BK;
+            const int gm = m0 + r, gk = k0 + k;
+            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : make_float2(0.f, 0.f);
+        }
+        for (int i = threadIdx.x; i < BK * BN; i += 256) {
+            const int k = i / BN, c = i % BN;
+            const int gk = k0 + k, gn = n0 + c;
+            Bs[k][c] = (gk < K && gn < N) ? B[(size_t)gk * N + gn] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < BK; ++k) {
+            float2 a[4];
+            float b[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) b[c] = Bs[k][tx * 4 + c];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    acc[r][c].x = fmaf(a[r].x, b[c], acc[r][c].x);
+                    acc[r][c].y = fmaf(a[r].y, b[c], acc[r][c].y);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int gm = m0 + ty * 4 + r, gn = n0 + tx * 4 + c;
+            if (gm < M && gn < N) Cm[(size_t)gm * N + gn] = acc[r][c];
+        }
+}
+
+// per plane z: C_z[M][N] (complex) = A[M][K] (real, row-major) . B_z[K][N] (complex)
+__global__ void __launch_bounds__(256) k_gemm_rc(const float *__restrict__ A, const float2 *__restrict__ B,
+                                                 float2 *__restrict__ Cm, int M, int N, int K) {
+    __shared__ float As[BK][BM + 4];
+    __shared__ float2 Bs[BK][BN + 1];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const size_t plane = (size_t)blockIdx.z;
+    const float2 *Bz = B + plane * (size_t)K * N;
+    float2 *Cz = Cm + plane * (size_t)M * N;
+    float2 acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        for (int i = threadIdx.x; i < BM * BK; i += 256) {
+            const int r = i / BK, k = i % BK;
+            const int gm = m0 + r, gk = k0 + k;
+            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : 0.f;
+        }
+        for (int i = threadIdx.x; i < BK * BN; i += 256) {
+            const int k = i / BN, c = i % BN;
+            const int gk = k0 + k, gn = n0 + c;
+            Bs[k][c] = (gk < K && gn < N) ? Bz[(size_t)gk * N + gn] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < BK; ++k) {
+            float a[4];
+            float2 b[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) b[c] = Bs[k][tx * 4 + c];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    acc[r][c].x = fmaf(a[r], b[c].x, acc[r][c].x);
+                    acc[r][c].y = fmaf(a[r], b[c].y, acc[r][c].y);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int gm = m0 + ty * 4 + r, gn = n0 + tx * 4 + c;
+            if (gm < M && gn < N) Cz[(size_t)gm * N + gn] = acc[r][c];
+        }
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 crecf(float2 a) {
+    const float d = 1.f / (a.x * a.x + a.y * a.y);
+    return make_float2(a.x * d, -a.y * d);
+}
+
+struct ZSolveParams {
+    float2 *x;              // in/out, shape (n2, n1, n0)
+    float2 *U;              // scratch: [k][q][line], q = 0..P
+    const float *bands;     // outer base bands [nb][n2][bw]
+    const float *lx, *ly;   // inner eigenvalues
+    int n0, n1, n2;
+    CombP<float> Bc, Cc;    // A_z(s) = Bc + s Cc
+};
+
+// one banded complex LU (no pivoting) + solve per line (i, j)
+template <int P>
+__global__ void k_zsolve(const ZSolveParams prm) {
+    constexpr int BWd = 2 * P + 1;
+    const int nl = prm.n0 * prm.n1;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nl) return;
+    const int i = l % prm.n0, j = l / prm.n0;
+    const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
+    const size_t stride = (size_t)nl;
+    float2 *x = prm.x + l;
+    float2 Uw[P][P + 1];     // U rows k-1 .. k-P
+    float2 yw[P];            // transformed rhs k-1 .. k-P
+#pragma unroll
+    for (int d = 0; d < P; ++d) {
+        yw[d] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q <= P; ++q) Uw[d][q] = make_float2(1.f, 0.f);
+    }
+    const int n = prm.n2;
+    for (int k = 0; k < n; ++k) {
+        float2 a[BWd];
+#pragma unroll
+        for (int o = 0; o < BWd; ++o) {
+            const float2 b = comb_at<float, float2>(prm.Bc, prm.bands, n, BWd, k, o);
+            const float2 c = comb_at<float, float2>(prm.Cc, prm.bands, n, BWd, k, o);
+            a[o] = make_float2(b.x + s * c.x, b.y + s * c.y);
+        }
+        float2 rhs = x[(size_t)k * stride];
+        // eliminate columns k-P .. k-1 with U rows k-P .. k-1
+#pragma unroll
+        for (int d = P; d >= 1; --d) {
+            if (k - d < 0) continue;
+            const float2 *Ur = Uw[d - 1];   // row k-d: Ur[q] = U(k-d, k-d+q)
+            const float2 f = cmulf(a[P - d], crecf(Ur[0]));
+#pragma unroll
+            for (int q = 1; q <= P; ++q) {
+                const int col = P - d + q;    // column k-d+q in a (< 2P+1)
+                const float2 t = cmulf(f, Ur[q]);
+                a[col].x -= t.x;
+                a[col].y -= t.y;
+            }
+            const float2 t = cmulf(f, yw[d - 1]);
+            rhs.x -= t.x;
+            rhs.y -= t.y;
+        }
+        // shift windows, store U row k
+#pragma unroll
+        for (int d = P - 1; d > 0; --d) {
+            yw[d] = yw[d - 1];
+#pragma unroll
+            for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
+        }
+#pragma unroll
+        for (int q = 0; q <= P; ++q) {
+            Uw[0][q] = a[P + q];
+            prm.U[((size_t)k * (P + 1) + q) * stride + l] = a[P + q];
+        }
+        yw[0] = rhs;
+        x[(size_t)k * stride] = rhs;
+    }
+    // back substitution
+    float2 xw[P];
+#pragma unroll
+    for (int d = 0; d < P; ++d) xw[d] = make_float2(0.f, 0.f);
+    for (int k = n - 1; k >= 0; --k) {
+        float2 v = x[(size_t)k * stride];
+#pragma unroll
+        for (int q = 1; q <= P; ++q) {
+            if (k + q >= n) continue;
+            const float2 t = cmulf(prm.U[((size_t)k * (P + 1) + q) * stride + l], xw[q - 1]);
+            v.x -= t.x;
+            v.y -= t.y;
+        }
+        v = cmulf(v, crecf(prm.U[((size_t)k * (P + 1)) * stride + l]));
+#pragma unroll
+        for (int d = P - 1; d > 0; --d) xw[d] = xw[d - 1];
+        xw[0] = v;
+        x[(size_t)k * stride] = v;
+    }
+}
+
+CombP<float> eval_combf(const Comb &c, const std::array<cd, 5> &sg, cd extra_scale = 1.0) {
+    CombP<float> out{};
+    out.n = c.n;
+    for (int i = 0; i < c.n; ++i) {
+        const cd v = c.factor[i] * sg[c.scalar[i]] * extra_scale;
+        out.base[i] = c.base[i];
+        out.re[i] = (float)v.real();
+        out.im[i] = (float)v.imag();
+    }
+    return out;
+}
+
+}  // namespace
+
+void PcFDM::setup(Operator *op_) {
+    op = op_;
+    const Space &s = *op->sp;
+    dim = s.dim;
+    TDZ_CHECK(dim >= 2, TDZ_ERR_UNSUPPORTED, "the FDM preconditioner needs 2D or 3D");
+    P = s.ax[0].p;
+    TDZ_CHECK(P >= 2 && P <= 5, TDZ_ERR_UNSUPPORTED, "the FDM preconditioner supports degrees 2..5");
+    const Plan &pl = op->plan(TDZ_STAGE);
+    // inner one-axis terms must be a common multiple of the stiffness
+    exact = true;
+    auto pure_s = [&](const Comb &c) {
+        for (int i = 0; i < c.n; ++i)
+            if (c.base[i] != kS) return false;
+        return true;
+    };
+    if (pl.hasB && (!pure_s(pl.xT) || (dim == 3 && !pure_s(pl.yT)))) exact = false;
+    for (int d = 0; d < 3; ++d) n[d] = d < dim ? s.ax[d].n : 1;
+    N = (size_t)s.ndof();
+    for (int d = 0; d < dim - 1; ++d) {
+        std::vector<double> Vd, ld;
+        gen_eig(op->bases[d][kS], op->bases[d][kM], Vd, ld);
+        const int nd = n[d];
+        std::vector<float> v32(Vd.begin(), Vd.end()), vt32((size_t)nd * nd), l32(ld.begin(), ld.end());
+        for (int i = 0; i < nd; ++i)
+            for (int j = 0; j < nd; ++j) vt32[(size_t)j * nd + i] = (float)Vd[(size_t)i * nd + j];
+        upload(V[d], v32);
+        upload(VT[d], vt32);
+        upload(lam[d], l32);
+    }
+    b1.alloc(N * sizeof(float2));
+    b2.alloc(N * sizeof(float2));
+    ufac.alloc(N * (P + 1) * sizeof(float2));
+}
+
+void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
+    const Plan &pl = op->plan(TDZ_STAGE);
+    const std::array<cd, 5> &sg = op->sigma;
+    const int outer = dim - 1;
+    float2 *x1 = b1.as<float2>(), *x2 = b2.as<float2>();
+    blas::cast(r, TDZ_FP64, x1, TDZ_FP32, N, st);
+    const int rows = n[1] * n[2];
+    // forward transforms: along x with V (t_i = sum_i' V[i'][i] r_i'), along y with V^T
+    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (rows + BM - 1) / BM), 256, 0, st>>>(x1, V[0].as<float>(), x2, rows, n[0], n[0]);
+    float2 *cur = x2, *oth = x1;
+    if (dim == 3) {
+        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(VT[1].as<float>(), x2, x1,
+                                                                                        n[1], n[0], n[1]);
+        cur = x1;
+        oth = x2;
+    }
+    TDZ_CUDA(cudaGetLastError());
+    // line solves along the outer axis: A_z(s) = zA + s (beta M + zC)
+    ZSolveParams zp{};
+    zp.x = cur;
+    zp.U = ufac.as<float2>();
+    zp.bands = op->dev32[outer].as<float>();
+    zp.lx = lam[0].as<float>();
+    zp.ly = dim == 3 ? lam[1].as<float>() : nullptr;
+    zp.n0 = n[0];
+    zp.n1 = dim == 3 ? n[1] : 1;
+    zp.n2 = n[outer];
+    zp.Bc = eval_combf(pl.zA, sg);
+    Comb cc = pl.zC;
+    if (pl.hasB && pl.xT.n > 0) {
+        // stream B: M_out (x) (M_y (x) beta S_x + beta S_y (x) M_x) -> beta M_out
+        cd beta = 0.0;
+        for (int t = 0; t < pl.xT.n; ++t)
+            if (pl.xT.base[t] == kS) beta += pl.xT.factor[t] * sg[pl.xT.scalar[t]];
+        cc.add(kM, 0, 0.0);
+        CombP<float> c = eval_combf(cc, sg);
+        for (int t = 0; t < c.n; ++t)
+            if (c.base[t] == kM) { c.re[t] += (float)beta.real(); c.im[t] += (float)beta.imag(); }
+        zp.Cc = c;
+    } else {
+        zp.Cc = eval_combf(cc, sg);
+    }
+    const int nl = zp.n0 * zp.n1;
+    switch (P) {
+    case 2: k_zsolve<2><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
+    case 3: k_zsolve<3><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
+    case 4: k_zsolve<4><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
+    case 5: k_zsolve<5><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
+    }
+    TDZ_CUDA(cudaGetLastError());
+    // inverse transforms: along y with V, along x with V^T
+    if (dim == 3) {
+        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(V[1].as<float>(), cur, oth,
+                                                                                        n[1], n[0], n[1]);
+        std::swap(cur, oth);
+    }
+    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (rows + BM - 1) / BM), 256, 0, st>>>(cur, VT[0].as<float>(), oth, rows, n[0], n[0]);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch(dim == 3 ? 5 : 3);
+    blas::cast(oth, TDZ_FP32, z, TDZ_FP64, N, st);
+    ++applies;
+}
+
+}  // namespace tdz

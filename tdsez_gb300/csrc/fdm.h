@@ -1,0 +1,35 @@
+// Fast-diagonalisation preconditioner for operators whose inner axes carry
+// only mass and stiffness (the z-layered structure). Internal.
+#pragma once
+
+#include <vector>
+
+#include "krylov.h"
+
+namespace tdz {
+
+// Generalised symmetric eigenproblem S V = M V diag(lam), V^T M V = I
+// (dense, host, FP64; Cholesky reduction + cyclic Jacobi).
+void gen_eig(const BandD &S, const BandD &M, std::vector<double> &V, std::vector<double> &lam);
+
+// A = (M_x (x) M_y) (x) Bz + (S_x (x) M_y + M_x (x) S_y) (x) Cz with Bz, Cz
+// combinations of the outer-axis base bands. Then
+//   A^-1 = (V_x (x) V_y (x) I) [ (Bz + (lam_i + lam_j) Cz)^-1 ]_{ij} (V_x^T (x) V_y^T (x) I),
+// applied as dense transforms along x and y and one banded complex LU solve
+// per (i, j) line along z, in FP32.
+struct PcFDM : Precond {
+    Operator *op = nullptr;
+    int dim = 0, P = 0;
+    int n[3] = {1, 1, 1};
+    size_t N = 0;
+    DevBuf V[2], VT[2];        // FP32 n_d x n_d (row-major) eigenvectors and their transpose
+    DevBuf lam[2];             // FP32 eigenvalues per inner axis
+    DevBuf zb;                 // FP32 outer base bands (a copy of the operator's)
+    DevBuf b1, b2, ufac;       // FP32 work vectors and the U factors of the line solves
+    bool exact = true;         // false: inner one-axis terms other than stiffness were dropped
+    long long applies = 0;
+    void setup(Operator *op_);
+    void apply(const double2 *r, double2 *z, cudaStream_t st) override;
+};
+
+}  // namespace tdz

@@ -27,6 +27,12 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     const int m = restart;
     const double bnorm = blas::nrm2(red, b, n, TDZ_FP64, st);
     s.bnorm = bnorm;
+    if (!std::isfinite(bnorm)) {
+        s.reason = -9;
+        s.rnorm = bnorm;
+        last = s;
+        return s;
+    }
     if (bnorm == 0.0) {
         blas::zero(x, n, TDZ_FP64, st);
         s.reason = 1;
@@ -42,7 +48,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     while (true) {
         // r = b - A x  -> V0
         double2 *v0 = V[0].as<double2>();
-        op->apply(TDZ_STAGE, TDZ_FP64, x, v0, st);
+        op->apply(TDZ_STAGE, aprec, x, v0, st);
         ++applies;
         blas::axpby(v0, 1.0, b, -1.0, n, TDZ_FP64, st);
         const double beta = blas::nrm2(red, v0, n, TDZ_FP64, st);
@@ -60,7 +66,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             double2 *zj = Z[j].as<double2>();
             pc->apply(V[j].as<double2>(), zj, st);
             double2 *wv = w.as<double2>();
-            op->apply(TDZ_STAGE, TDZ_FP64, zj, wv, st);
+            op->apply(TDZ_STAGE, aprec, zj, wv, st);
             ++applies;
             // CGS with one re-orthogonalisation
             blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h.data(), st);

@@ -45,6 +45,7 @@ struct FGMRES {
     blas::Reducer red;
     SolveStats last;
     long long applies = 0;
+    int aprec = TDZ_FP64;   // operator apply arithmetic: TDZ_FP64 or TDZ_FP64_DF (FP64 vectors either way)
 
     void setup(Operator *op_, int restart_, Precond *pc_);
     // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.

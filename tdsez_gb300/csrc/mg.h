@@ -39,14 +39,15 @@ struct MGLevel {
     int n[3] = {1, 1, 1};
     size_t ndof = 0;
     DevBuf x, b, r, d, z, t1, t2;         // working precision vectors
-    double mu_lo = 0.0, mu_hi = 0.0;      // spectrum of M^-1 H_E on this level
+    double mu_lo = 0.0, mu_hi = 0.0;      // spectrum of M^-1 H_E on this level (real part; hi = |mu|max)
+    double w_max = 0.0;                   // bound on its imaginary extent (CAP)
 };
 
 struct MGOptions {
     int levels = 0;          // 0 = until < 2000 DoFs (MGLevels = 0)
-    int smooth = 2;          // Chebyshev degree of pre and post smoothing
+    int smooth = 8;          // Chebyshev degree of pre and post smoothing
     int coarse_its = 12;     // Chebyshev degree of the coarsest solve
-    double ratio = 6.0;      // smoothing range [mu_hi / ratio, mu_hi]
+    double ratio = 60.0;     // smoothing range [mu_hi / ratio, mu_hi]
     int precision = TDZ_FP32;
 };
 

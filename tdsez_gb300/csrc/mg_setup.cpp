@@ -268,6 +268,7 @@ void Multigrid::estimate_bounds(cudaStream_t st) {
             blas::axpby(m.x.ptr, cd(1.0 / std::max(nt, 1e-300)), m.t1.ptr, 0.0, m.ndof, prec, st);
         }
         m.mu_lo = m.mu_hi - 1.05 * lam2;
+        m.w_max = fine->cap_bound;
         op.sigma = saved;
     }
 }
@@ -276,13 +277,24 @@ void Multigrid::refresh() {}
 
 namespace {
 
-// Chebyshev iteration on A x = b with M^-1, spectral segment
-// alpha + g [mu_a, mu_b]; x_zero: x starts at 0.
-void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, int steps, bool x_zero, cudaStream_t st) {
+// Chebyshev iteration on A x = b with M^-1. The eigenvalues of M^-1 A are
+// alpha + g mu with mu = mu_r - i mu_i, mu_r in [mu_a, mu_b] (Hermitian part)
+// and mu_i in [0, w] (CAP). The iteration uses the ellipse that encloses this
+// rectangle (semi-axes sqrt2 times its half-sides; the segment itself when
+// w = 0): center theta and focal half-distance delta in the lambda-plane.
+// x_zero: x starts at 0.
+void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, double w, int steps, bool x_zero, cudaStream_t st) {
     Operator &op = *m.opp;
     const cd alpha = op.sigma[0], g = op.sigma[1];
-    const cd theta = alpha + g * (0.5 * (mu_a + mu_b));
-    const cd delta = g * (0.5 * (mu_b - mu_a));
+    const cd center = cd(0.5 * (mu_a + mu_b), -0.5 * w);
+    cd focal;
+    if (w <= 0.0) focal = cd(0.5 * (mu_b - mu_a), 0.0);
+    else {
+        const double a = std::sqrt(2.0) * 0.5 * (mu_b - mu_a), b = std::sqrt(2.0) * 0.5 * w;
+        focal = a >= b ? cd(std::sqrt(a * a - b * b), 0.0) : cd(0.0, -std::sqrt(b * b - a * a));
+    }
+    const cd theta = alpha + g * center;
+    const cd delta = g * focal;
     const size_t n = m.ndof;
     // r = b - A x
     if (x_zero) blas::copy(m.b.ptr, m.r.ptr, n, prec, st);
@@ -323,11 +335,11 @@ void Multigrid::vcycle(int l, cudaStream_t st) {
     MGLevel &m = lv[l];
     const int last = (int)lv.size() - 1;
     if (l == last) {
-        chebyshev(m, prec, m.mu_lo, m.mu_hi, opt.coarse_its, true, st);
+        chebyshev(m, prec, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);
         return;
     }
     const double lo = m.mu_hi / opt.ratio;
-    chebyshev(m, prec, lo, m.mu_hi, opt.smooth, true, st);
+    chebyshev(m, prec, lo, m.mu_hi, m.w_max, opt.smooth, true, st);
     // r = b - A x
     m.opp->apply(TDZ_STAGE, prec, m.x.ptr, m.t1.ptr, st);
     blas::axpbypcz(m.r.ptr, 1.0, m.b.ptr, 0.0, m.t1.ptr, -1.0, m.ndof, prec, st);
@@ -358,7 +370,7 @@ void Multigrid::vcycle(int l, cudaStream_t st) {
         src = dst;
         ti ^= 1;
     }
-    chebyshev(m, prec, lo, m.mu_hi, opt.smooth, false, st);
+    chebyshev(m, prec, lo, m.mu_hi, m.w_max, opt.smooth, false, st);
 }
 
 void Multigrid::apply(const double2 *r, double2 *z, cudaStream_t st) {

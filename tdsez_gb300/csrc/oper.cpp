@@ -85,7 +85,14 @@ void Operator::build(const Space &s, const tdz_physics &ph) {
             b[d] = add_band(d, s.ax[d].band(ph.pot_q[d], 0, 0));
             terms.push_back({1, cd(sgn), b});
         }
-    // CAP
+    // CAP; its Rayleigh quotient against M is bounded by the largest profile value
+    cap_bound = 0.0;
+    for (int d = 0; d < dim; ++d)
+        if (ph.cap_q[d]) {
+            double mx = 0.0;
+            for (size_t k = 0; k < s.ax[d].xq.size(); ++k) mx = std::max(mx, std::abs(ph.cap_q[d][k]));
+            cap_bound += mx * std::abs(ph.cap_inv_mass);
+        }
     for (int d = 0; d < dim; ++d)
         if (ph.cap_q[d]) {
             auto b = base_bands();
@@ -172,11 +179,17 @@ std::array<cd, 5> Operator::sigma_for(int which) const {
 void Operator::upload_bases() {
     for (int d = 0; d < sp->dim; ++d) {
         std::vector<double> v64;
-        std::vector<float> v32;
+        std::vector<float> v32, vdf;   // vdf: (hi, lo) pairs, hi + lo = v to about 48 bits
         for (const BandD &b : bases[d])
-            for (double v : b.v) { v64.push_back(v); v32.push_back((float)v); }
+            for (double v : b.v) {
+                v64.push_back(v);
+                v32.push_back((float)v);
+                vdf.push_back((float)v);
+                vdf.push_back((float)(v - (double)(float)v));
+            }
         upload(dev64[d], v64);
         upload(dev32[d], v32);
+        upload(devdf[d], vdf);
     }
 }
 
@@ -242,7 +255,8 @@ void Operator::set_stage(cd alpha, cd g, const std::vector<cd> &c) {
 }
 
 void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t st) {
-    TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64, TDZ_ERR_ARG, "precision must be TDZ_FP32 or TDZ_FP64");
+    TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG,
+              "precision must be TDZ_FP32, TDZ_FP64 or TDZ_FP64_DF");
     TDZ_CHECK(x && y, TDZ_ERR_ARG, "null vector");
     TDZ_CHECK(x != y, TDZ_ERR_ARG, "x and y must not alias");
     if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");

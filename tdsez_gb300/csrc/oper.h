@@ -52,9 +52,10 @@ struct Operator {
     tdz_physics phys{};
     int P = 0;                                  // common degree (2D/3D kernels)
     std::array<std::vector<BandD>, 3> bases;    // base bands per axis
-    std::array<DevBuf, 3> dev32, dev64;         // base bands on the device per axis
+    std::array<DevBuf, 3> dev32, dev64, devdf;  // base bands on the device per axis (FP32, FP64, double-float)
     std::vector<Term> terms;                    // all terms of the stage operator
     std::vector<int> coupled;                   // coupled axes in order
+    double cap_bound = 0.0;                     // bound on the CAP part of M^-1 H (Rayleigh quotient)
     // 1D Dirichlet walls: wall diagonal of H and M
     bool wall1d = false;
     double h_wall[2] = {0, 0}, m_wall[2] = {0, 0};

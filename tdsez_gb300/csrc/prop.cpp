@@ -11,6 +11,8 @@
 // (src/propagator.cpp:729-758).
 #include "prop.h"
 
+#include "fdm.h"
+
 #include <cmath>
 
 namespace tdz {
@@ -56,8 +58,14 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
         mo.precision = o.pc_precision;
         p->setup(op, mo, st);
         pc = std::move(p);
+    } else if (o.pc == 3) {
+        auto p = std::make_unique<PcFDM>();
+        p->setup(op);
+        pc = std::move(p);
     } else throw Error(TDZ_ERR_ARG, "unknown preconditioner");
     ksp.setup(op, restart, pc.get());
+    TDZ_CHECK(o.outer == TDZ_FP64 || o.outer == TDZ_FP64_DF, TDZ_ERR_ARG, "outer precision must be FP64 or FP64_DF");
+    ksp.aprec = o.outer;
 }
 
 SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st) {
@@ -83,6 +91,7 @@ void Propagator::setup(Operator *op_, int kind_, const SolverOptions &o, int gue
     // preconditioners are built from the stage of the first step
     // (src/propagator.cpp:446-460); the multigrid follows later stage changes
     nsolvers = kind == 0 ? 1 : 2;
+    aprec = o.outer;
     for (int k = 0; k < nsolvers; ++k) solver[k].setup(op, o, st);
 }
 
@@ -122,7 +131,7 @@ void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t s
 
 void Propagator::cn_step(double2 *psi, double h, const std::vector<cd> &c, cudaStream_t st) {
     op->set_stage(1.0, cd(0.0, 0.5 * h), c);
-    op->apply(TDZ_MASS, TDZ_FP64, psi, rhs.ptr, st);          // M psi
+    op->apply(TDZ_MASS, aprec, psi, rhs.ptr, st);          // M psi
     double2 *X = tmp.as<double2>();
     blas::copy(psi, X, n, TDZ_FP64, st);
     extrapolate(0, X, st);
@@ -137,8 +146,8 @@ void Propagator::pade_step(double2 *psi, double h, const std::vector<cd> &c, int
     for (int k = 0; k < 2; ++k) {
         // rhs = (M + conj(g_k) H_E) x = 2 M x - A_{1-k} x
         op->set_stage(1.0, g[1 - k], c);
-        op->apply(TDZ_STAGE, TDZ_FP64, psi, tmp.ptr, st);
-        op->apply(TDZ_MASS, TDZ_FP64, psi, rhs.ptr, st);
+        op->apply(TDZ_STAGE, aprec, psi, tmp.ptr, st);
+        op->apply(TDZ_MASS, aprec, psi, rhs.ptr, st);
         blas::axpby(rhs.ptr, -1.0, tmp.ptr, 2.0, n, TDZ_FP64, st);
         blas::copy(psi, x0.ptr, n, TDZ_FP64, st);               // stage input
         const int s = 2 * slot + k;

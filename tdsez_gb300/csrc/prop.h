@@ -16,6 +16,7 @@ struct SolverOptions {
     double rtol = 1e-12;
     int pc = 2;           // 0 none, 1 Kronecker mass, 2 multigrid
     int pc_precision = TDZ_FP32;
+    int outer = TDZ_FP64;  // operator applies of FGMRES and the right-hand sides (TDZ_FP64 or TDZ_FP64_DF)
     MGOptions mg;
 };
 
@@ -58,6 +59,7 @@ struct PCRefresh {
 
 struct Propagator {
     Operator *op = nullptr;
+    int aprec = TDZ_FP64;         // arithmetic of the right-hand-side applies
     int kind = 0;                 // TDZ_CN, TDZ_PADE22, TDZ_MAGNUS4
     Solver solver[2];             // one per stage shift (CN: one)
     int nsolvers = 1;

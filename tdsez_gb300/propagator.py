@@ -18,13 +18,18 @@ from . import _lib
 from .operators import Operator
 
 KINDS = {"cn": _lib.TDZ_CN, "pade22": _lib.TDZ_PADE22, "magnus4": _lib.TDZ_MAGNUS4}
-PCS = {"none": _lib.TDZ_PC_NONE, "mass": _lib.TDZ_PC_MASS, "mg": _lib.TDZ_PC_MG}
+PCS = {"none": _lib.TDZ_PC_NONE, "mass": _lib.TDZ_PC_MASS, "mg": _lib.TDZ_PC_MG, "fdm": _lib.TDZ_PC_FDM}
 S3 = math.sqrt(3.0)
 MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 
 
 def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
-                maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 2, mg_coarse_its: int = 12):
+                maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 0, mg_coarse_its: int = 12,
+                outer: str = "fp64"):
+    """Solver options. ``precision`` is the preconditioner's arithmetic
+    (fp32 = mixed precision); ``outer`` the arithmetic of the FP64 Krylov
+    method's operator applies: "fp64" (native) or "df" (double-float on the
+    FP32 pipes, about 48 significant bits)."""
     o = _lib.tdz_solver_opts()
     o.restart = restart
     o.maxit = maxit
@@ -34,6 +39,7 @@ def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, re
     o.mg_levels = mg_levels
     o.mg_smooth = mg_smooth
     o.mg_coarse_its = mg_coarse_its
+    o.outer_precision = {"fp64": _lib.TDZ_FP64, "df": _lib.TDZ_FP64_DF}[outer]
     return o
 
 

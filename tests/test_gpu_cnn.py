@@ -32,7 +32,7 @@ def test_cnn_gradients_match_oracle(cuda):
     import torch
     from tdsez_gb300 import _lib
     lib = _lib.load()
-    cin, width, cout, L, D, H, W, B = 4, 8, 2, 3, 5, 6, 7, 2
+    cin, width, cout, L, D, H, W, B = 4, 16, 2, 3, 9, 6, 8, 2
     h = C.c_void_p()
     _lib.check(lib.tdz_cnn_create(cin, width, cout, L, D, H, W, B, 7, C.byref(h)))
     n = C.c_longlong()
@@ -41,6 +41,7 @@ def test_cnn_gradients_match_oracle(cuda):
     params = (0.2 * rng.standard_normal(n.value)).astype(np.float32)
     _lib.check(lib.tdz_cnn_set_params(h, params.ctypes.data_as(C.POINTER(C.c_float))))
     shapes = [(width, cin), (width, width), (cout, width)]
+    assert sum(co * ci * 27 + co for co, ci in shapes) == n.value
     Ws, bs = _unpack(params.astype(np.float64), shapes)
     Wq = [bf16(w) for w in Ws]          # the kernels multiply by BF16 weights
     x = rng.standard_normal((B, cin, D, H, W)).astype(np.float32)
@@ -60,9 +61,63 @@ def test_cnn_gradients_match_oracle(cuda):
     _lib.check(lib.tdz_cnn_get_grads(h, g.ctypes.data_as(C.POINTER(C.c_float))))
     Lref, gW, gb = ocnn.loss_and_grads(x.astype(np.float64), t.astype(np.float64), Wq, bs)
     assert abs(loss.value - Lref) <= 1e-4 * Lref
-    gref = np.concatenate([np.concatenate([w.reshape(-1), b]) for w, b in zip(gW, gb)])
-    # data gradients pass through BF16 (flipped) weights: a few 1e-3 relative
-    assert np.linalg.norm(g - gref) <= 1e-2 * np.linalg.norm(gref)
+    # per layer: weights and bias gradients (data gradients pass through BF16
+    # flipped weights: a few 1e-3 relative)
+    o = 0
+    for l, ((co, ci), w, b) in enumerate(zip(shapes, gW, gb)):
+        nw = co * ci * 27
+        gw_gpu, gb_gpu = g[o:o + nw], g[o + nw:o + nw + co]
+        o += nw + co
+        ew = np.linalg.norm(gw_gpu - w.reshape(-1)) / np.linalg.norm(w)
+        eb = np.linalg.norm(gb_gpu - b) / max(np.linalg.norm(b), 1e-30)
+        assert ew <= 1e-2 and eb <= 1e-2, (l, ew, eb)
+    lib.tdz_cnn_destroy(h)
+
+
+@pytest.mark.gpu
+def test_cnn_adam_steps_match_oracle(cuda):
+    """Three Adam steps (lr 3e-3) on the GPU against the same steps in numpy
+    (FP64 master weights, BF16-rounded weights in the forward pass): the
+    parameter updates agree."""
+    import torch
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    cin, width, cout, L, D, H, W, B = 2, 16, 2, 3, 8, 8, 8, 4
+    h = C.c_void_p()
+    _lib.check(lib.tdz_cnn_create(cin, width, cout, L, D, H, W, B, 3, C.byref(h)))
+    n = C.c_longlong()
+    _lib.check(lib.tdz_cnn_num_params(h, C.byref(n)))
+    p0 = np.zeros(n.value, dtype=np.float32)
+    _lib.check(lib.tdz_cnn_get_params(h, p0.ctypes.data_as(C.POINTER(C.c_float))))
+    shapes = [(width, cin), (width, width), (cout, width)]
+    params = [a.copy() for a in _unpack(p0.astype(np.float64), shapes)[0]] + \
+        [a.copy() for a in _unpack(p0.astype(np.float64), shapes)[1]]
+    m = [np.zeros_like(a) for a in params]
+    v = [np.zeros_like(a) for a in params]
+    rng = np.random.default_rng(4)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lr = 3e-3
+    for it in range(1, 4):
+        x = rng.standard_normal((B, cin, D, H, W)).astype(np.float32)
+        t = rng.standard_normal((B, cout, D, H, W)).astype(np.float32)
+        xd, td = torch.tensor(x, device=cuda), torch.tensor(t, device=cuda)
+        _lib.check(lib.tdz_cnn_train_step(h, C.c_void_p(xd.data_ptr()), C.c_void_p(td.data_ptr()), B, lr, s))
+        Ws, bs = params[:L], params[L:]
+        _, gW, gb = ocnn.loss_and_grads(x.astype(np.float64), t.astype(np.float64), [bf16(w) for w in Ws], bs)
+        for i, g in enumerate(gW + gb):
+            m[i] = 0.9 * m[i] + 0.1 * g
+            v[i] = 0.999 * v[i] + 0.001 * g * g
+            params[i] = params[i] - lr * (m[i] / (1 - 0.9 ** it)) / (np.sqrt(v[i] / (1 - 0.999 ** it)) + 1e-8)
+        pg = np.zeros(n.value, dtype=np.float32)
+        torch.cuda.synchronize()
+        _lib.check(lib.tdz_cnn_get_params(h, pg.ctypes.data_as(C.POINTER(C.c_float))))
+        Wg, bg = _unpack(pg.astype(np.float64), shapes)
+        W0, b0 = _unpack(p0.astype(np.float64), shapes)
+        for l in range(L):
+            dg, dn = Wg[l] - W0[l], params[l] - W0[l]
+            assert np.linalg.norm(dg - dn) <= 0.05 * np.linalg.norm(dn), ("W", it, l, np.linalg.norm(dg - dn) / np.linalg.norm(dn))
+            dg, dn = bg[l] - b0[l], params[L + l] - b0[l]
+            assert np.linalg.norm(dg - dn) <= 0.05 * np.linalg.norm(dn) + 1e-7, ("b", it, l)
     lib.tdz_cnn_destroy(h)
 
 

@@ -13,12 +13,22 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
+def _berr(Am, x, b):
+    """Normwise backward error ||b - A x|| / (||b|| + || |A| |x| ||): the
+    measure that does not charge the solver for the rounding-level difference
+    between the oracle's assembled matrix and the library's operator, which
+    ||A|| ||x|| / ||b|| magnifies for stiff (high-degree) cases."""
+    return np.linalg.norm(b - Am @ x) / (np.linalg.norm(b) + np.linalg.norm(abs(Am) @ np.abs(x)))
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["3d_heterostructure", "3d_const_mass_cap", "2d_cap_softcore_sep", "3d_p2_hole"])
-@pytest.mark.parametrize("pc,prec", [("mg", "fp32"), ("mg", "fp64"), ("mass", "fp32"), ("mass", "fp64")])
-def test_stage_solve_parity(cuda, name, pc, prec):
+@pytest.mark.parametrize("pc,prec,outer", [("mg", "fp32", "fp64"), ("mg", "fp64", "fp64"), ("mass", "fp32", "fp64"),
+                                           ("mass", "fp64", "fp64"), ("mg", "fp32", "df")])
+def test_stage_solve_parity(cuda, name, pc, prec, outer):
     """FGMRES + (mixed-precision) preconditioner reaches the FP64 solution of
-    (M + i tau H_E) x = b: true residual of the oracle matrix <= 1e-11."""
+    (M + i tau H_E) x = b: true residual of the oracle matrix <= 1e-11, also
+    when the Krylov method's applies run in double-float arithmetic."""
     import torch
     from tdsez_gb300.propagator import Solver
     c = CASES[name]()
@@ -31,7 +41,7 @@ def test_stage_solve_parity(cuda, name, pc, prec):
     rng = np.random.default_rng(3)
     b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
     xref = sla.spsolve(Am, b)
-    s = Solver(op, pc=pc, precision=prec, rtol=1e-12, maxit=400)
+    s = Solver(op, pc=pc, precision=prec, rtol=1e-12, maxit=400, outer=outer)
     bd = torch.tensor(b, device=cuda)
     xd = torch.zeros_like(bd)
     its, reason, rn = s.solve(bd, xd)
@@ -40,7 +50,37 @@ def test_stage_solve_parity(cuda, name, pc, prec):
     assert np.linalg.norm(b - Am @ x) / np.linalg.norm(b) < 1e-11
     assert _rel(x, xref) < 1e-9
     if pc == "mg":
-        assert its <= 60, its
+        # 3d_const_mass_cap has under 2000 DoFs: one level, whose coarse solve
+        # is the Chebyshev polynomial (the reference factorises it with LU)
+        assert its <= (100 if name == "3d_const_mass_cap" else 60), its
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_p2_hole", "3d_p5_sym", "2d_cap_softcore_sep"])
+def test_fdm_solve(cuda, name):
+    """Fast-diagonalisation preconditioner: exact (FP32) for operators whose
+    inner axes carry only mass and stiffness (heterostructure), approximate
+    otherwise; FGMRES reaches the FP64 solution either way."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    tau = 0.2
+    cc = [0.02 * (k + 1) for k in range(len(c["coupled"]))]
+    op.set_stage(1.0, 1j * tau, cc)
+    Am = (A.M + 1j * tau * (A.H_total() + sum(ck * T for ck, T in zip(cc, A.terms())))).tocsc()
+    rng = np.random.default_rng(8)
+    b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    s = Solver(op, pc="fdm", precision="fp32", rtol=1e-12, maxit=400)
+    bd = torch.tensor(b, device=cuda)
+    xd = torch.zeros_like(bd)
+    its, reason, rn = s.solve(bd, xd)
+    x = xd.cpu().numpy()
+    assert reason > 0, (its, reason, rn)
+    assert _berr(Am, x, b) < 1e-12, _berr(Am, x, b)
+    if name == "3d_heterostructure":
+        assert its <= 4, its            # exact inverse up to FP32: one digit group per iteration
 
 
 @pytest.mark.gpu
