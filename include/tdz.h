@@ -204,6 +204,19 @@ tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n,
 tdz_status tdz_vec_mdot_noalloc(const void *const *V, int k, const void *w, long long n, int precision, void *out,
                                 void *stream);
 
+/* Batched complex-by-real transform on the tensor cores (tcgen05, TF32 with
+ * a three-term split: FP32-class accuracy), the eigenvector transform of the
+ * fast-diagonalisation preconditioner; the counterpart of the per-axis
+ * contraction of TDSEZTensorOps::Term (src/tensorops.cpp:97-153) for a dense
+ * matrix:
+ *   out[((p N + n) 2 + c) ldo + r] = sum_k in[((p R + r) 2 + c) ldi + k] B[k N + n]
+ * for planes p < planes, rows r < R, parts c (0 real, 1 imaginary), n < N <= 256.
+ * B: K x N row-major FP64 host matrix; in/out: FP32 device arrays, 16-byte
+ * aligned, ldi a multiple of 4 and >= K, ldo >= R. Uploads B on every call
+ * (set-up and tests; the preconditioner keeps its matrices resident). */
+tdz_status tdz_plane_transform(const double *B, int K, int N, const float *in, int planes, int R, int ldi, float *out,
+                               int ldo, void *stream);
+
 /* ----------------------------------------------------------- propagator
  * Time steps of TDSEZPropagator::Evolve (CN, src/propagator.cpp:78-251) and
  * EvolveRational / Pade22Step (src/propagator.cpp:564-769) on a device state

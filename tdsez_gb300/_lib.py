@@ -114,6 +114,7 @@ SIGNATURES = {
     "tdz_tsurff_amplitudes": (I, [VP, C.POINTER(D), VP]),
     "tdz_tsurff_volkov": (I, [VP, C.POINTER(D)]),
     "tdz_tsurff_destroy": (None, [VP]),
+    "tdz_plane_transform": (I, [C.POINTER(C.c_double), I, I, VP, I, I, I, VP, I, VP]),
     "tdz_cnn_create": (I, [I, I, I, I, I, I, I, I, C.c_ulonglong, PP]),
     "tdz_cnn_forward": (I, [VP, VP, VP, I, VP]),
     "tdz_cnn_train_step": (I, [VP, VP, VP, I, C.c_float, VP]),

@@ -12,6 +12,7 @@
 
 #include "oper.h"
 #include "prop.h"
+#include "tgemm.h"
 #include "tsurff.h"
 #include "cnn.h"
 
@@ -259,6 +260,20 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
               "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;
+}
+
+tdz_status tdz_plane_transform(const double *B, int K, int N, const float *in, int planes, int R, int ldi, float *out,
+                               int ldo, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(B && in && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(K >= 1 && N >= 1 && planes >= 1 && R >= 1, TDZ_ERR_ARG, "sizes must be positive");
+        TDZ_CHECK(ldi % 4 == 0 && ldi >= K && ldo >= R, TDZ_ERR_ARG, "bad pitches");
+        tdz::TransformMat T;
+        T.build(std::vector<double>(B, B + (size_t)K * N), K, N);
+        tdz::transform(T, in, planes, R, ldi, out, ldo, static_cast<cudaStream_t>(stream));
+        TDZ_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+        TDZ_CHECK(tdz::take_transform_error() == 0, TDZ_ERR_CUDA, "tensor-core transform: a bounded wait ran out");
+    });
 }
 
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out) {

@@ -212,8 +212,31 @@ __device__ __forceinline__ float2 crecf(float2 a) {
     return make_float2(a.x * d, -a.y * d);
 }
 
+// natural-order complex FP64 -> row-planar FP32 [z][y][c][x] (row pitch ld)
+__global__ void k_to_planar(const double2 *__restrict__ r, float *__restrict__ a, int n0, size_t rows, int ld) {
+    const size_t total = rows * (size_t)n0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = e / n0;
+        const int x = (int)(e % n0);
+        const double2 v = r[e];
+        a[(row * 2) * ld + x] = (float)v.x;
+        a[(row * 2 + 1) * ld + x] = (float)v.y;
+    }
+}
+
+__global__ void k_from_planar(const float *__restrict__ a, double2 *__restrict__ z, int n0, size_t rows, int ld) {
+    const size_t total = rows * (size_t)n0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = e / n0;
+        const int x = (int)(e % n0);
+        z[e] = make_double2((double)a[(row * 2) * ld + x], (double)a[(row * 2 + 1) * ld + x]);
+    }
+}
+
 struct ZSolveParams {
-    float2 *x;              // in/out, shape (n2, n1, n0)
+    float *x;               // in/out: real part of (line (i, j), row k) at x[k ks + j js + i is], imaginary at + cs
+    size_t ks;
+    int js, is, cs;
     float2 *U;              // scratch: [k][q][line], q = 0..P
     const float *bands;     // outer base bands [nb][n2][bw]
     const float *lx, *ly;   // inner eigenvalues
@@ -221,18 +244,41 @@ struct ZSolveParams {
     CombP<float> Bc, Cc;    // A_z(s) = Bc + s Cc
 };
 
-// one banded complex LU (no pivoting) + solve per line (i, j)
+// One banded complex LU (no pivoting) + solve per line (i, j), one thread
+// per line, lines contiguous in memory (coalesced across the warp). The
+// recursion along z is latency-bound, so (1) the line matrix bands
+// A_z(s) = Bc + s Cc are evaluated once per CTA into shared memory, (2) the
+// right-hand side rows are prefetched kDist rows ahead into a register ring,
+// and the back substitution prefetches its x and U rows the same way, and
+// (3) the U scratch keeps the reciprocal pivot, so each row costs one complex
+// reciprocal. Shared memory: 2 n2 (2P+1) float2 (the two band combinations).
+constexpr int kZDist = 8, kZDistB = 4;
+
 template <int P>
-__global__ void k_zsolve(const ZSolveParams prm) {
+__global__ void __launch_bounds__(128) k_zsolve(const ZSolveParams prm) {
     constexpr int BWd = 2 * P + 1;
+    extern __shared__ float2 zs_bands[];
+    float2 *sB = zs_bands, *sC = zs_bands + (size_t)prm.n2 * BWd;
+    const int n = prm.n2;
+    for (int e = threadIdx.x; e < n * BWd; e += blockDim.x) {
+        const int k = e / BWd, o = e % BWd;
+        sB[e] = comb_at<float, float2>(prm.Bc, prm.bands, n, BWd, k, o);
+        sC[e] = comb_at<float, float2>(prm.Cc, prm.bands, n, BWd, k, o);
+    }
+    __syncthreads();
     const int nl = prm.n0 * prm.n1;
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nl) return;
     const int i = l % prm.n0, j = l / prm.n0;
     const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
     const size_t stride = (size_t)nl;
-    float2 *x = prm.x + l;
-    float2 Uw[P][P + 1];     // U rows k-1 .. k-P
+    float *xl = prm.x + (size_t)j * prm.js + (size_t)i * prm.is;
+    const size_t ks = prm.ks;
+    const int cs = prm.cs;
+    auto ldx = [&](int k) { const float *q = xl + (size_t)k * ks; return make_float2(q[0], q[cs]); };
+    auto stx = [&](int k, float2 v) { float *q = xl + (size_t)k * ks; q[0] = v.x; q[cs] = v.y; };
+    float2 *U = prm.U + l;
+    float2 Uw[P][P + 1];     // U rows k-1 .. k-P; [0] holds the reciprocal pivot
     float2 yw[P];            // transformed rhs k-1 .. k-P
 #pragma unroll
     for (int d = 0; d < P; ++d) {
@@ -240,67 +286,106 @@ __global__ void k_zsolve(const ZSolveParams prm) {
 #pragma unroll
         for (int q = 0; q <= P; ++q) Uw[d][q] = make_float2(1.f, 0.f);
     }
-    const int n = prm.n2;
-    for (int k = 0; k < n; ++k) {
-        float2 a[BWd];
+    float2 pf[kZDist];
 #pragma unroll
-        for (int o = 0; o < BWd; ++o) {
-            const float2 b = comb_at<float, float2>(prm.Bc, prm.bands, n, BWd, k, o);
-            const float2 c = comb_at<float, float2>(prm.Cc, prm.bands, n, BWd, k, o);
-            a[o] = make_float2(b.x + s * c.x, b.y + s * c.y);
-        }
-        float2 rhs = x[(size_t)k * stride];
-        // eliminate columns k-P .. k-1 with U rows k-P .. k-1
+    for (int u = 0; u < kZDist; ++u) pf[u] = u < n ? ldx(u) : make_float2(0.f, 0.f);
+    for (int k0 = 0; k0 < n; k0 += kZDist) {
 #pragma unroll
-        for (int d = P; d >= 1; --d) {
-            if (k - d < 0) continue;
-            const float2 *Ur = Uw[d - 1];   // row k-d: Ur[q] = U(k-d, k-d+q)
-            const float2 f = cmulf(a[P - d], crecf(Ur[0]));
+        for (int u = 0; u < kZDist; ++u) {
+            const int k = k0 + u;
+            if (k < n) {
+                float2 rhs = pf[u];
+                if (k + kZDist < n) pf[u] = ldx(k + kZDist);
+                float2 a[BWd];
 #pragma unroll
-            for (int q = 1; q <= P; ++q) {
-                const int col = P - d + q;    // column k-d+q in a (< 2P+1)
-                const float2 t = cmulf(f, Ur[q]);
-                a[col].x -= t.x;
-                a[col].y -= t.y;
+                for (int o = 0; o < BWd; ++o) {
+                    const float2 b = sB[k * BWd + o], c = sC[k * BWd + o];
+                    a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
+                }
+                // eliminate columns k-P .. k-1 with U rows k-P .. k-1
+#pragma unroll
+                for (int d = P; d >= 1; --d) {
+                    if (k - d < 0) continue;
+                    const float2 *Ur = Uw[d - 1];   // row k-d: Ur[q] = U(k-d, k-d+q), Ur[0] = 1 / U(k-d, k-d)
+                    const float2 f = cmulf(a[P - d], Ur[0]);
+#pragma unroll
+                    for (int q = 1; q <= P; ++q) {
+                        const float2 t = cmulf(f, Ur[q]);
+                        a[P - d + q].x -= t.x;
+                        a[P - d + q].y -= t.y;
+                    }
+                    const float2 t = cmulf(f, yw[d - 1]);
+                    rhs.x -= t.x;
+                    rhs.y -= t.y;
+                }
+                a[P] = crecf(a[P]);
+#pragma unroll
+                for (int d = P - 1; d > 0; --d) {
+                    yw[d] = yw[d - 1];
+#pragma unroll
+                    for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
+                }
+#pragma unroll
+                for (int q = 0; q <= P; ++q) {
+                    Uw[0][q] = a[P + q];
+                    U[((size_t)k * (P + 1) + q) * stride] = a[P + q];
+                }
+                yw[0] = rhs;
+                stx(k, rhs);
             }
-            const float2 t = cmulf(f, yw[d - 1]);
-            rhs.x -= t.x;
-            rhs.y -= t.y;
         }
-        // shift windows, store U row k
-#pragma unroll
-        for (int d = P - 1; d > 0; --d) {
-            yw[d] = yw[d - 1];
-#pragma unroll
-            for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
-        }
-#pragma unroll
-        for (int q = 0; q <= P; ++q) {
-            Uw[0][q] = a[P + q];
-            prm.U[((size_t)k * (P + 1) + q) * stride + l] = a[P + q];
-        }
-        yw[0] = rhs;
-        x[(size_t)k * stride] = rhs;
     }
-    // back substitution
+    // back substitution, rows n-1 .. 0, prefetching kZDistB rows ahead
     float2 xw[P];
 #pragma unroll
     for (int d = 0; d < P; ++d) xw[d] = make_float2(0.f, 0.f);
-    for (int k = n - 1; k >= 0; --k) {
-        float2 v = x[(size_t)k * stride];
+    float2 px[kZDistB], pu[kZDistB][P + 1];
 #pragma unroll
-        for (int q = 1; q <= P; ++q) {
-            if (k + q >= n) continue;
-            const float2 t = cmulf(prm.U[((size_t)k * (P + 1) + q) * stride + l], xw[q - 1]);
-            v.x -= t.x;
-            v.y -= t.y;
-        }
-        v = cmulf(v, crecf(prm.U[((size_t)k * (P + 1)) * stride + l]));
+    for (int u = 0; u < kZDistB; ++u) {
+        const int k = n - 1 - u;
+        px[u] = k >= 0 ? ldx(k) : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int d = P - 1; d > 0; --d) xw[d] = xw[d - 1];
-        xw[0] = v;
-        x[(size_t)k * stride] = v;
+        for (int q = 0; q <= P; ++q) pu[u][q] = k >= 0 ? U[((size_t)k * (P + 1) + q) * stride] : make_float2(0.f, 0.f);
     }
+    for (int k0 = n - 1; k0 >= 0; k0 -= kZDistB) {
+#pragma unroll
+        for (int u = 0; u < kZDistB; ++u) {
+            const int k = k0 - u;
+            if (k >= 0) {
+                float2 v = px[u];
+                float2 ur[P + 1];
+#pragma unroll
+                for (int q = 0; q <= P; ++q) ur[q] = pu[u][q];
+                const int kn = k - kZDistB;
+                if (kn >= 0) {
+                    px[u] = ldx(kn);
+#pragma unroll
+                    for (int q = 0; q <= P; ++q) pu[u][q] = U[((size_t)kn * (P + 1) + q) * stride];
+                }
+#pragma unroll
+                for (int q = 1; q <= P; ++q) {
+                    if (k + q >= n) continue;
+                    const float2 t = cmulf(ur[q], xw[q - 1]);
+                    v.x -= t.x;
+                    v.y -= t.y;
+                }
+                v = cmulf(v, ur[0]);
+#pragma unroll
+                for (int d = P - 1; d > 0; --d) xw[d] = xw[d - 1];
+                xw[0] = v;
+                stx(k, v);
+            }
+        }
+    }
+}
+
+template <int P> void launch_zsolve(const ZSolveParams &zp, cudaStream_t st) {
+    const int nl = zp.n0 * zp.n1;
+    const size_t smem = (size_t)2 * zp.n2 * (2 * P + 1) * sizeof(float2);
+    TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
+    if (smem > 48 * 1024)
+        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_zsolve<P><<<(nl + 127) / 128, 128, smem, st>>>(zp);
 }
 
 CombP<float> eval_combf(const Comb &c, const std::array<cd, 5> &sg, cd extra_scale = 1.0) {
@@ -335,46 +420,53 @@ void PcFDM::setup(Operator *op_) {
     if (pl.hasB && (!pure_s(pl.xT) || (dim == 3 && !pure_s(pl.yT)))) exact = false;
     for (int d = 0; d < 3; ++d) n[d] = d < dim ? s.ax[d].n : 1;
     N = (size_t)s.ndof();
+    tensor = dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);
     for (int d = 0; d < dim - 1; ++d) {
         std::vector<double> Vd, ld;
         gen_eig(op->bases[d][kS], op->bases[d][kM], Vd, ld);
         const int nd = n[d];
-        std::vector<float> v32(Vd.begin(), Vd.end()), vt32((size_t)nd * nd), l32(ld.begin(), ld.end());
+        std::vector<double> VTd((size_t)nd * nd);
         for (int i = 0; i < nd; ++i)
-            for (int j = 0; j < nd; ++j) vt32[(size_t)j * nd + i] = (float)Vd[(size_t)i * nd + j];
-        upload(V[d], v32);
-        upload(VT[d], vt32);
+            for (int j = 0; j < nd; ++j) VTd[(size_t)j * nd + i] = Vd[(size_t)i * nd + j];
+        std::vector<float> v32(Vd.begin(), Vd.end()), vt32(VTd.begin(), VTd.end()), l32(ld.begin(), ld.end());
         upload(lam[d], l32);
+        if (tensor) {
+            // 3D: eigenvector transforms on the tensor cores (forward with V, inverse with V^T)
+            Tf[d].build(Vd, nd, nd);
+            Ti[d].build(VTd, nd, nd);
+        } else {
+            upload(V[d], v32);
+            upload(VT[d], vt32);
+        }
     }
-    b1.alloc(N * sizeof(float2));
-    b2.alloc(N * sizeof(float2));
     ufac.alloc(N * (P + 1) * sizeof(float2));
+    if (tensor) {
+        ldx = (n[0] + 3) / 4 * 4;
+        ldy = (n[1] + 3) / 4 * 4;
+        pa.alloc((size_t)n[2] * n[1] * 2 * ldx * sizeof(float));
+        pb.alloc((size_t)n[2] * n[0] * 2 * ldy * sizeof(float));
+    } else {
+        b1.alloc(N * sizeof(float2));
+        b2.alloc(N * sizeof(float2));
+    }
 }
 
-void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
-    const Plan &pl = op->plan(TDZ_STAGE);
+namespace {
+
+// line solve parameters of the current stage (bands and eigenvalues; the
+// caller sets the data layout)
+ZSolveParams line_params(const PcFDM &f) {
+    const Operator *op = f.op;
+    const int dim = f.dim;
+    const int *n = f.n;
+    const Plan &pl = const_cast<Operator *>(op)->plan(TDZ_STAGE);
     const std::array<cd, 5> &sg = op->sigma;
     const int outer = dim - 1;
-    float2 *x1 = b1.as<float2>(), *x2 = b2.as<float2>();
-    blas::cast(r, TDZ_FP64, x1, TDZ_FP32, N, st);
-    const int rows = n[1] * n[2];
-    // forward transforms: along x with V (t_i = sum_i' V[i'][i] r_i'), along y with V^T
-    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (rows + BM - 1) / BM), 256, 0, st>>>(x1, V[0].as<float>(), x2, rows, n[0], n[0]);
-    float2 *cur = x2, *oth = x1;
-    if (dim == 3) {
-        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(VT[1].as<float>(), x2, x1,
-                                                                                        n[1], n[0], n[1]);
-        cur = x1;
-        oth = x2;
-    }
-    TDZ_CUDA(cudaGetLastError());
-    // line solves along the outer axis: A_z(s) = zA + s (beta M + zC)
     ZSolveParams zp{};
-    zp.x = cur;
-    zp.U = ufac.as<float2>();
+    zp.U = f.ufac.as<float2>();
     zp.bands = op->dev32[outer].as<float>();
-    zp.lx = lam[0].as<float>();
-    zp.ly = dim == 3 ? lam[1].as<float>() : nullptr;
+    zp.lx = f.lam[0].as<float>();
+    zp.ly = dim == 3 ? f.lam[1].as<float>() : nullptr;
     zp.n0 = n[0];
     zp.n1 = dim == 3 ? n[1] : 1;
     zp.n2 = n[outer];
@@ -393,23 +485,78 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
     } else {
         zp.Cc = eval_combf(cc, sg);
     }
-    const int nl = zp.n0 * zp.n1;
+    return zp;
+}
+
+void line_solve(int P, const ZSolveParams &zp, cudaStream_t st) {
     switch (P) {
-    case 2: k_zsolve<2><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
-    case 3: k_zsolve<3><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
-    case 4: k_zsolve<4><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
-    case 5: k_zsolve<5><<<(nl + 127) / 128, 128, 0, st>>>(zp); break;
+    case 2: launch_zsolve<2>(zp, st); break;
+    case 3: launch_zsolve<3>(zp, st); break;
+    case 4: launch_zsolve<4>(zp, st); break;
+    case 5: launch_zsolve<5>(zp, st); break;
     }
     TDZ_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+}  // namespace
+
+void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
+    const size_t rows = (size_t)n[1] * n[2];
+    if (tensor) {
+        // [z][y][c][x] -> [z][x'][c][y] -> [z][y'][c][x'] -> line solves -> [z][x][c][y'] -> [z][y][c][x]
+        float *a = pa.as<float>(), *b = pb.as<float>();
+        const int blocks = (int)std::min<size_t>((N + 255) / 256, 152 * 16);
+        k_to_planar<<<blocks, 256, 0, st>>>(r, a, n[0], rows, ldx);
+        transform(Tf[0], a, n[2], n[1], ldx, b, ldy, st);
+        transform(Tf[1], b, n[2], n[0], ldy, a, ldx, st);
+        ZSolveParams zp = line_params(*this);
+        zp.x = a;
+        zp.ks = (size_t)2 * n[1] * ldx;
+        zp.js = 2 * ldx;
+        zp.is = 1;
+        zp.cs = ldx;
+        line_solve(P, zp, st);
+        transform(Ti[0], a, n[2], n[1], ldx, b, ldy, st);
+        transform(Ti[1], b, n[2], n[0], ldy, a, ldx, st);
+        k_from_planar<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx);
+        TDZ_CUDA(cudaGetLastError());
+        count_launch(2);
+        ++applies;
+        return;
+    }
+    float2 *x1 = b1.as<float2>(), *x2 = b2.as<float2>();
+    blas::cast(r, TDZ_FP64, x1, TDZ_FP32, N, st);
+    const int grows = (int)rows;
+    // forward transforms: along x with V (t_i = sum_i' V[i'][i] r_i'), along y with V^T
+    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (grows + BM - 1) / BM), 256, 0, st>>>(x1, V[0].as<float>(), x2, grows, n[0],
+                                                                                 n[0]);
+    float2 *cur = x2, *oth = x1;
+    if (dim == 3) {
+        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(VT[1].as<float>(), x2, x1,
+                                                                                        n[1], n[0], n[1]);
+        cur = x1;
+        oth = x2;
+    }
+    TDZ_CUDA(cudaGetLastError());
+    // line solves along the outer axis: A_z(s) = zA + s (beta M + zC), interleaved complex
+    ZSolveParams zp = line_params(*this);
+    zp.x = reinterpret_cast<float *>(cur);
+    zp.ks = (size_t)2 * n[0] * (dim == 3 ? n[1] : 1);
+    zp.js = 2 * n[0];
+    zp.is = 2;
+    zp.cs = 1;
+    line_solve(P, zp, st);
     // inverse transforms: along y with V, along x with V^T
     if (dim == 3) {
         k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(V[1].as<float>(), cur, oth,
                                                                                         n[1], n[0], n[1]);
         std::swap(cur, oth);
     }
-    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (rows + BM - 1) / BM), 256, 0, st>>>(cur, VT[0].as<float>(), oth, rows, n[0], n[0]);
+    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (grows + BM - 1) / BM), 256, 0, st>>>(cur, VT[0].as<float>(), oth, grows,
+                                                                                 n[0], n[0]);
     TDZ_CUDA(cudaGetLastError());
-    count_launch(dim == 3 ? 5 : 3);
+    count_launch(dim == 3 ? 4 : 2);
     blas::cast(oth, TDZ_FP32, z, TDZ_FP64, N, st);
     ++applies;
 }

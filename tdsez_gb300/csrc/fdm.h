@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "krylov.h"
+#include "tgemm.h"
 
 namespace tdz {
 
@@ -27,6 +28,12 @@ struct PcFDM : Precond {
     DevBuf zb;                 // FP32 outer base bands (a copy of the operator's)
     DevBuf b1, b2, ufac;       // FP32 work vectors and the U factors of the line solves
     bool exact = true;         // false: inner one-axis terms other than stiffness were dropped
+    // 3D with n_x, n_y <= 256: transforms on the tensor cores (tcgen05, TF32 x 3) over
+    // row-planar FP32 buffers pa ([z][y][c][x], pitch ldx) and pb ([z][x][c][y], pitch ldy)
+    bool tensor = false;
+    TransformMat Tf[2], Ti[2];
+    DevBuf pa, pb;
+    int ldx = 0, ldy = 0;
     long long applies = 0;
     void setup(Operator *op_);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;

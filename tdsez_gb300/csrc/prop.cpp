@@ -70,6 +70,8 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
 
 SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st) {
     SolveStats s = ksp.solve(b, x, opt.rtol, opt.maxit, st);
+    if (opt.pc == 3 && static_cast<PcFDM *>(pc.get())->tensor)
+        TDZ_CHECK(take_transform_error() == 0, TDZ_ERR_CUDA, "tensor-core transform: a bounded wait ran out");
     ++solves;
     its += s.its;
     return s;

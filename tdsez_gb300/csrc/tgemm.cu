@@ -1,0 +1,373 @@
+// tcgen05 transform kernel (see tgemm.h).
+//
+// One CTA of 128 threads computes a 128 x Np output tile (64 complex rows,
+// real and imaginary part rows interleaved) with the accumulator in tensor
+// memory (TMEM, Np <= 256 FP32 columns). K runs in chunks of 32 (one
+// 128-byte swizzled row per operand row) through a two-stage shared-memory
+// pipeline fed by TMA (cp.async.bulk.tensor, 128-byte swizzle):
+//   stage = A (128 x 32 FP32 -> split in place into TF32 hi + lo)
+//         + B hi, B lo (Np x 32 each, precomputed split).
+// Per 8-wide K step the elected thread issues three MMAs,
+//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi,
+// which keeps about 22 significant bits (the dropped A_lo B_lo term is
+// ~2^-22 relative), i.e. FP32-class results from TF32 tensor-core rates.
+// The epilogue reads TMEM with tcgen05.ld (warp w owns lanes 32w..32w+31,
+// lane = tile row) and stores the tile transposed per plane.
+// Every wait on an mbarrier is bounded (clock64): on time-out the kernel sets
+// the error word, skips the remaining MMAs and still frees its TMEM.
+#include "tgemm.h"
+
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace tdz {
+
+namespace {
+
+constexpr int TM = 128;        // tile rows (GEMM rows)
+constexpr int KC = 32;         // K per stage (128 bytes of FP32)
+constexpr int NSTAGE = 2;
+constexpr int A_BYTES = TM * KC * 4;   // 16 KB
+constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
+
+__device__ int g_tgemm_error = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) {
+            atomicExch(&g_tgemm_error, 1);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major operand in the canonical 128-byte
+// swizzled layout (8-row groups 1024 bytes apart), start address addr
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);          // start address >> 4      bits  0-13
+    d |= (uint64_t)1 << 16;                          // leading offset (unused) bits 16-29
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride offset 1024 B    bits 32-45
+    d |= (uint64_t)1 << 46;                          // descriptor version      bits 46-47
+    d |= (uint64_t)2 << 61;                          // 128-byte swizzle        bits 61-63
+    return d;
+}
+
+// instruction descriptor: kind::tf32, FP32 accumulator, K-major A and B, M = 128
+__host__ __device__ constexpr uint32_t instr_desc(int n) {
+    return (1u << 4)                         // D format F32
+           | (2u << 7)                       // A format TF32
+           | (2u << 10)                      // B format TF32
+           | ((uint32_t)(n >> 3) << 17)      // N >> 3
+           | ((uint32_t)(TM >> 4) << 24);    // M >> 4
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ float tf32_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
+
+struct TGParams {
+    float *out;
+    int rows;      // GEMM rows = 2 planes R
+    int R, N, ldo, nchunks;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(128, 1)
+    k_transform(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap, const TGParams prm) {
+    constexpr int B_BYTES = NP * KC * 4;
+    constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    constexpr uint32_t TMEM_COLS = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;
+    static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N tile");
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + NSTAGE * STAGE);   // full[2], done[2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NSTAGE);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TM;
+    const int nch = prm.nchunks;
+    auto a_hi = [&](int s) { return base + s * STAGE; };
+    auto a_lo = [&](int s) { return base + s * STAGE + A_BYTES; };
+    auto b_hi = [&](int s) { return base + s * STAGE + 2 * A_BYTES; };
+    auto b_lo = [&](int s) { return base + s * STAGE + 2 * A_BYTES + B_BYTES; };
+    const uint32_t full0 = smem_u32(&bars[0]), done0 = smem_u32(&bars[NSTAGE]);
+
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(done0 + 8 * s, 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = instr_desc(NP);
+    constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
+    bool ok = true;
+
+    auto issue = [&](int c, int s) {
+        mbar_expect_tx(full0 + 8 * s, TX);
+        tma_load_2d(smem_u32(a_hi(s)), &amap, c * KC, m0, full0 + 8 * s);
+        tma_load_2d(smem_u32(b_hi(s)), &bmap, c * KC, 0, full0 + 8 * s);
+        tma_load_2d(smem_u32(b_lo(s)), &bmap, c * KC, NP, full0 + 8 * s);
+    };
+    if (tid == 0) issue(0, 0);
+    for (int c = 0; c < nch; ++c) {
+        const int s = c & 1;
+        if (tid == 0 && c + 1 < nch) {
+            const int s1 = (c + 1) & 1;
+            if (c >= 1) ok = ok && mbar_wait(done0 + 8 * s1, ((c - 1) >> 1) & 1);
+            if (ok) issue(c + 1, s1);
+        }
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        if (!mbar_wait(full0 + 8 * s, (c >> 1) & 1)) ok = false;
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        // split A into TF32 hi (in place) and lo
+        float4 *ah = reinterpret_cast<float4 *>(a_hi(s));
+        float4 *al = reinterpret_cast<float4 *>(a_lo(s));
+#pragma unroll
+        for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
+            const int e = tid + q * 128;
+            const float4 v = ah[e];
+            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+            ah[e] = h;
+            al[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah_a = smem_u32(a_hi(s)), al_a = smem_u32(a_lo(s));
+            const uint32_t bh_a = smem_u32(b_hi(s)), bl_a = smem_u32(b_lo(s));
+#pragma unroll
+            for (int j = 0; j < KC / 8; ++j) {
+                const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the swizzled row
+                const uint64_t dah = smem_desc(ah_a + off), dal = smem_desc(al_a + off);
+                const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
+                mma_tf32(tmem, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                mma_tf32(tmem, dah, dbl, idesc, 1u);
+                mma_tf32(tmem, dal, dbh, idesc, 1u);
+            }
+            mma_commit(done0 + 8 * s);
+        }
+    }
+    // all MMAs done: the last commit covers every earlier MMA of the thread
+    if (ok) ok = mbar_wait(done0 + 8 * ((nch - 1) & 1), ((nch - 1) >> 1) & 1);
+    ok = __syncthreads_and(ok) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int g = m0 + warp * 32 + lane;   // this thread's tile row
+        const bool row_ok = g < prm.rows;
+        const int cr = g >> 1, part = g & 1;
+        const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
+        float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
+        const size_t nstride = (size_t)2 * prm.ldo;
+#pragma unroll 1
+        for (int c0 = 0; c0 < NP; c0 += 16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row_ok) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = c0 + j;
+                    if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    TDZ_CHECK(fn != nullptr, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+
+// 2D FP32 tensor map: inner extent `inner` (elements), `outer` rows of pitch
+// `pitch` elements, box 32 x box_rows, 128-byte swizzle, zero fill outside
+void make_map(CUtensorMap *map, const void *ptr, uint64_t inner, uint64_t outer, uint64_t pitch, uint32_t box_rows) {
+    TDZ_CHECK((reinterpret_cast<uintptr_t>(ptr) & 15) == 0, TDZ_ERR_ARG, "transform operand not 16-byte aligned");
+    TDZ_CHECK((pitch * 4) % 16 == 0, TDZ_ERR_ARG, "transform row pitch not a multiple of 16 bytes");
+    const cuuint64_t dims[2] = {inner, outer};
+    const cuuint64_t strides[1] = {pitch * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)KC, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(ptr), dims, strides,
+                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TDZ_CHECK(r == CUDA_SUCCESS, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+float tf32_trunc_host(double v) {
+    float f = (float)v;
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u &= 0xFFFFE000u;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+template <int NP> void launch(const TransformMat &T, const CUtensorMap &amap, const TGParams &prm, int tiles,
+                              cudaStream_t st) {
+    constexpr int STAGE = 2 * A_BYTES + 2 * NP * KC * 4;
+    const size_t smem = 1024 + (size_t)NSTAGE * STAGE + 2 * NSTAGE * 8 + 16;
+    static bool attr = false;   // set once per process (same device attribute for every device)
+    if (!attr) {
+        TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    k_transform<NP><<<tiles, 128, smem, st>>>(amap, T.map, prm);
+}
+
+}  // namespace
+
+bool transform_supported(int N) { return N >= 1 && N <= 256; }
+
+void TransformMat::build(const std::vector<double> &B, int K_, int N_) {
+    K = K_;
+    N = N_;
+    TDZ_CHECK(transform_supported(N), TDZ_ERR_UNSUPPORTED, "tensor-core transform supports N <= 256");
+    TDZ_CHECK((int)B.size() == K * N, TDZ_ERR_ARG, "transform matrix size");
+    Kp = (K + KC - 1) / KC * KC;
+    Np = (N + 15) / 16 * 16;
+    std::vector<float> h((size_t)2 * Np * Kp, 0.f);
+    for (int n = 0; n < N; ++n)
+        for (int k = 0; k < K; ++k) {
+            const double v = B[(size_t)k * N + n];
+            const float hi = tf32_trunc_host(v);
+            h[(size_t)n * Kp + k] = hi;
+            h[(size_t)(Np + n) * Kp + k] = tf32_trunc_host(v - (double)hi);
+        }
+    upload(hilo, h);
+    make_map(&map, hilo.ptr, Kp, 2 * (uint64_t)Np, Kp, (uint32_t)Np);
+}
+
+int take_transform_error() {
+    int h = 0;
+    TDZ_CUDA(cudaMemcpyFromSymbol(&h, g_tgemm_error, sizeof(int)));
+    if (h) {
+        const int z = 0;
+        TDZ_CUDA(cudaMemcpyToSymbol(g_tgemm_error, &z, sizeof(int)));
+    }
+    return h;
+}
+
+void transform(const TransformMat &T, const float *in, int planes, int R, int ldi, float *out, int ldo,
+               cudaStream_t st) {
+    TDZ_CHECK(ldi >= T.K && ldo >= R, TDZ_ERR_ARG, "transform pitches too small");
+    const long long rows = 2LL * planes * R;
+    TDZ_CHECK(rows < (1LL << 31), TDZ_ERR_ARG, "transform too large");
+    CUtensorMap amap;
+    make_map(&amap, in, (uint64_t)T.K, (uint64_t)rows, (uint64_t)ldi, TM);
+    TGParams prm{};
+    prm.out = out;
+    prm.rows = (int)rows;
+    prm.R = R;
+    prm.N = T.N;
+    prm.ldo = ldo;
+    prm.nchunks = T.Kp / KC;
+    const int tiles = (int)((rows + TM - 1) / TM);
+    switch (T.Np) {
+    case 16: launch<16>(T, amap, prm, tiles, st); break;
+    case 32: launch<32>(T, amap, prm, tiles, st); break;
+    case 48: launch<48>(T, amap, prm, tiles, st); break;
+    case 64: launch<64>(T, amap, prm, tiles, st); break;
+    case 80: launch<80>(T, amap, prm, tiles, st); break;
+    case 96: launch<96>(T, amap, prm, tiles, st); break;
+    case 112: launch<112>(T, amap, prm, tiles, st); break;
+    case 128: launch<128>(T, amap, prm, tiles, st); break;
+    case 144: launch<144>(T, amap, prm, tiles, st); break;
+    case 160: launch<160>(T, amap, prm, tiles, st); break;
+    case 176: launch<176>(T, amap, prm, tiles, st); break;
+    case 192: launch<192>(T, amap, prm, tiles, st); break;
+    case 208: launch<208>(T, amap, prm, tiles, st); break;
+    case 224: launch<224>(T, amap, prm, tiles, st); break;
+    case 240: launch<240>(T, amap, prm, tiles, st); break;
+    case 256: launch<256>(T, amap, prm, tiles, st); break;
+    default: throw Error(TDZ_ERR_INTERNAL, "bad transform tile width");
+    }
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
+}
+
+}  // namespace tdz

@@ -123,7 +123,10 @@ def test_cnn_adam_steps_match_oracle(cuda):
 
 @pytest.mark.gpu
 def test_cnn_training_lowers_loss(cuda):
-    """Adam on a smoothing target (the network learns a fixed 3D stencil)."""
+    """Adam on a smoothing target (the network learns a fixed 3D stencil).
+    lr 1e-3: at 3e-3 the same network, replayed in numpy from five random
+    initialisations, collapses to the zero output (relative loss 1) in four
+    of them; at 1e-3 all five reach about 0.15 in 150 steps."""
     import torch
     from tdsez_gb300 import _lib
     lib = _lib.load()
@@ -137,7 +140,7 @@ def test_cnn_training_lowers_loss(cuda):
         x = torch.randn((B, cin, D, H, W), generator=g).to(cuda)
         k = torch.ones((cin, 1, 3, 3, 3), device=cuda) / 27.0
         t = torch.nn.functional.conv3d(x, k, padding=1, groups=cin)
-        _lib.check(lib.tdz_cnn_train_step(h, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), B, 3e-3, s))
+        _lib.check(lib.tdz_cnn_train_step(h, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), B, 1e-3, s))
         if it % 10 == 9:
             v = C.c_float()
             _lib.check(lib.tdz_cnn_loss(h, C.byref(v), s))
