@@ -152,6 +152,8 @@ def run_tdz(args):
               mg_levels=args.mg_levels)
     if args.apply_only:
         return apply_only(args, op, S, psi0, stream)
+    if args.precond_only:
+        return precond_only(args, op, S, psi0, stream, w)
 
     # ---- headline arm: FP64 FGMRES, FP32 preconditioner (fast diagonalisation)
     t_setup = time.time()
@@ -299,6 +301,19 @@ def apply_only(args, op, S, psi0, stream):
                       "apply_df_us": tdf * 1e6, "apply_df_gbs": 32.0 * N / tdf / 1e9, "N": N}))
 
 
+def precond_only(args, op, S, psi0, stream, w):
+    """Time one FDM preconditioner application (transforms + line solves) on
+    the CN stage, args.steps applications after 3 warm-up ones; restart 2 keeps
+    the device footprint small (the command profiled for the FDM kernels)."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    op.set_stage(1.0, 0.5j * w.dt, [0.001])
+    s = Solver(op, pc="fdm", precision="fp32", restart=2, rtol=1e-10)
+    z = torch.empty_like(psi0)
+    t = time_kernel(lambda: s.precondition(psi0, z), args.steps, stream)
+    print(json.dumps({"fdm_apply_us": t * 1e6, "N": S.ndof}))
+
+
 def cpu_baseline(n_full: int, dt: float, seconds: float):
     """The oracle's CPU path (scipy GMRES + ILU on the assembled FP64 CN
     matrix, the reference's method restated) on a reduced grid of the same
@@ -338,6 +353,7 @@ def main():
     ap.add_argument("--pc", default="fdm")
     ap.add_argument("--outer", default="df", choices=["df", "fp64"])
     ap.add_argument("--apply-only", action="store_true")
+    ap.add_argument("--precond-only", action="store_true")
     ap.add_argument("--mg-smooth", type=int, default=8)
     ap.add_argument("--mg-coarse-its", type=int, default=12)
     ap.add_argument("--mg-levels", type=int, default=0)

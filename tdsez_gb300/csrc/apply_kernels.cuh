@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "cplx.cuh"
 #include "oper.h"
@@ -54,7 +55,7 @@ __device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, 
         z.x = tfma(cb.re[t], b, z.x);
         z.y = tfma(cb.im[t], b, z.y);
     }
-    return z;
+    return cnorm(z);
 }
 
 // ---------------------------------------------------------------- 3D kernel
@@ -65,14 +66,17 @@ __device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, 
 // double-buffered, so two barriers per plane suffice.
 constexpr int kLoadsPerThread3 = 4;   // covers (TY+2p)(TX+2p) / (TX TY) for p <= 5
 
+// TX is the largest tile width; the launch may use a narrower one
+// (blockDim.x = 16..TX) to fit n0 with less padding.
 template <class T, int P, bool HB, bool HC, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     using C = typename CT<T>::type;
     constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
     constexpr int NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
     constexpr int UT = 1, US = HB ? 2 : 1;    // slots of u_T and u_S in sU
-    constexpr int NT = TX * TY;
-    static_assert(RY * RX <= kLoadsPerThread3 * NT, "tile larger than the prefetch registers");
+    static_assert(RY * (16 + 2 * P) <= kLoadsPerThread3 * 16 * TY, "tile larger than the prefetch registers");
+    const int txw = blockDim.x;               // tile width of this launch
+    const int NT = txw * TY, RXw = txw + 2 * P;
     __shared__ C sIn[RY][RX];
     __shared__ C sU[2][NU][RY][TX];
     __shared__ T sYm[BW][TY];
@@ -84,10 +88,10 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     C *sZC = sZA + (size_t)prm.zchunk_planes * BW;
     T *sZM = reinterpret_cast<T *>(sZC + (HC ? (size_t)prm.zchunk_planes * BW : 0));
 
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * txw + tx;
     const int n0 = prm.n0, n1 = prm.n1, n2 = prm.n2;
-    const int tilesX = (n0 + TX - 1) / TX;
-    const int x0 = (blockIdx.x % tilesX) * TX, y0 = (blockIdx.x / tilesX) * TY;
+    const int tilesX = (n0 + txw - 1) / txw;
+    const int x0 = (blockIdx.x % tilesX) * txw, y0 = (blockIdx.x / tilesX) * TY;
     const int gx = x0 + tx, gy = y0 + ty;
     const int z0 = blockIdx.y * prm.zchunk;
     const int z1 = min(n2, z0 + prm.zchunk);
@@ -130,8 +134,8 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
         for (int q = 0; q < kLoadsPerThread3; ++q) {
             const int e = tid + q * NT;
             C v = czero<C>();
-            if (e < RY * RX) {
-                const int r = e / RX, c = e % RX;
+            if (e < RY * RXw) {
+                const int r = e / RXw, c = e % RXw;
                 const int yy = y0 - P + r, xx = x0 - P + c;
                 if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) v = load_c<C>(X[((size_t)zin * n1 + yy) * n0 + xx]);
             }
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
 #pragma unroll
                 for (int q = 0; q < kLoadsPerThread3; ++q) {
                     const int e = tid + q * NT;
-                    if (e < RY * RX) sIn[e / RX][e % RX] = pre[q];
+                    if (e < RY * RXw) sIn[e / RXw][e % RXw] = pre[q];
                 }
                 __syncthreads();
                 if (zin + 1 < n2 && zin + 1 < z1 + P) load_plane(zin + 1);
@@ -170,9 +174,9 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
                         if constexpr (HB) cfma(uT, xt[j], v);
                         if constexpr (HC) rfma(uS, xs[j], v);
                     }
-                    sU[buf][0][r][tx] = uM;
-                    if constexpr (HB) sU[buf][UT][r][tx] = uT;
-                    if constexpr (HC) sU[buf][US][r][tx] = uS;
+                    sU[buf][0][r][tx] = cnorm(uM);
+                    if constexpr (HB) sU[buf][UT][r][tx] = cnorm(uT);
+                    if constexpr (HC) sU[buf][US][r][tx] = cnorm(uS);
                 }
                 __syncthreads();
                 // y stage
@@ -191,6 +195,9 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
                         rfma(wC, sYs[j][ty], um);
                     }
                 }
+                wA = cnorm(wA);
+                if constexpr (HB) wB = cnorm(wB);
+                if constexpr (HC) wC = cnorm(wC);
                 // outer (z) stage
                 const C *zA = sZA + (size_t)it * BW;
 #pragma unroll
@@ -268,6 +275,9 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
                     if constexpr (HB) cfma(uT, xt[j], v);
                     if constexpr (HC) rfma(uS, xs[j], v);
                 }
+                uM = cnorm(uM);
+                if constexpr (HB) uT = cnorm(uT);
+                if constexpr (HC) uS = cnorm(uS);
 #pragma unroll
                 for (int o = 0; o < BW; ++o) {
                     C &a = acc[(ph - P + o + 2 * BW) % BW];
@@ -316,27 +326,41 @@ __global__ void k_apply1d(const ApplyParams<T> prm) {
 // ---------------------------------------------------------------- launch helpers
 constexpr int kTX3 = 32, kTY3 = 8, kTX2 = 128;
 
-inline int pick_chunk(int tiles, int n_outer, int P) {
-    // about 8 CTAs per SM over 152 SMs; chunks no shorter than 4p planes
-    const int target = 152 * 8;
+// z chunk per CTA: about `target` CTAs in total, chunks no shorter than 4p
+// planes (the 2p halo planes of a chunk are re-read and, in the compute-bound
+// double-float kernel, recomputed)
+inline int pick_chunk(int tiles, int n_outer, int P, int target = 152 * 8) {
     int chunks = (target + tiles - 1) / tiles;
     chunks = std::max(1, std::min(chunks, n_outer / std::max(1, 4 * P)));
     return (n_outer + chunks - 1) / chunks;
+}
+
+// tile width 16..32 (multiple of 4) with the least padding of n0; ties go to the wider
+inline int pick_tile_x(int n0) {
+    int best = kTX3, pad = (n0 + kTX3 - 1) / kTX3 * kTX3;
+    for (int t = kTX3 - 4; t >= 16; t -= 4) {
+        const int p = (n0 + t - 1) / t * t;
+        if (p < pad) { pad = p; best = t; }
+    }
+    return best;
 }
 
 template <class T, int P, bool HB, bool HC>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     using C = typename CT<T>::type;
     ApplyParams<T> prm = prm0;
-    const int tiles = ((prm.n0 + kTX3 - 1) / kTX3) * ((prm.n1 + kTY3 - 1) / kTY3);
-    prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P), 96);
+    const int txw = pick_tile_x(prm.n0);
+    const int tiles = ((prm.n0 + txw - 1) / txw) * ((prm.n1 + kTY3 - 1) / kTY3);
+    // compute-bound double-float: about two waves of two CTAs per SM; otherwise about 8 CTAs per SM
+    const int target = std::is_same<T, float>::value ? 152 * 8 : 152 * 4;
+    prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P, target), 96);
     prm.zchunk_planes = prm.zchunk + 2 * P;
     const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
     const size_t smem = rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
     auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
     if (smem > 48 * 1024) TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
-    kern<<<grid, dim3(kTX3, kTY3), smem, st>>>(prm);
+    kern<<<grid, dim3(txw, kTY3), smem, st>>>(prm);
 }
 
 template <class T, int P, bool HB, bool HC>

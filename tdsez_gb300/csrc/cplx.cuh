@@ -7,11 +7,13 @@ namespace tdz {
 // Double-float: a value hi + lo carried as two FP32 numbers (about 48
 // significant bits; Dekker 1971, as in the double-double arithmetic of Hida,
 // Li and Bailey 2001 with single-precision halves). The product a.hi b.hi is
-// split exactly with an fma residual, the sum uses Knuth's two-sum error term
-// and one renormalisation. Every step is an explicitly rounded intrinsic, so
-// the compiler cannot contract or reorder it. An accumulation of a few dozen
-// terms keeps a relative error near 1e-14 while running on the FP32 pipes,
-// which on this GPU are 64x the FP64 rate.
+// split exactly with an fma residual, the sum uses Knuth's two-sum error term.
+// Accumulations skip the per-term renormalisation: lo collects the product
+// and rounding errors of a whole banded sum (a few dozen terms, so it stays
+// far below hi's last bit times the term count) and renorm() folds it into
+// hi once per stage result. Every step is an explicitly rounded intrinsic, so
+// the compiler cannot contract or reorder it. Relative error near 1e-14 on
+// the FP32 pipes, which on this GPU run at 64x the FP64 rate.
 struct dff {
     float hi, lo;
     dff() = default;
@@ -25,7 +27,7 @@ __device__ __forceinline__ dff operator-(dff a) { return dff(-a.hi, -a.lo); }
 // a * b + c in the arithmetic type of the operands
 __device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double tfma(double a, double b, double c) { return ::fma(a, b, c); }
-// double-float (13 FP32 instructions)
+// double-float, unnormalised result (12 FP32 instructions)
 __device__ __forceinline__ dff tfma(dff a, dff b, dff c) {
     const float p = __fmul_rn(a.hi, b.hi);
     float e = __fmaf_rn(a.hi, b.hi, -p);
@@ -34,10 +36,12 @@ __device__ __forceinline__ dff tfma(dff a, dff b, dff c) {
     const float s = __fadd_rn(c.hi, p);
     const float bv = __fsub_rn(s, c.hi);
     const float err = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
-    float lo = __fadd_rn(__fadd_rn(c.lo, e), err);
-    const float h2 = __fadd_rn(s, lo);
-    lo = __fsub_rn(lo, __fsub_rn(h2, s));
-    return dff(h2, lo);
+    return dff(s, __fadd_rn(__fadd_rn(c.lo, e), err));
+}
+// fold lo into hi (fast two-sum; |lo| <= |hi| for an accumulated value)
+__device__ __forceinline__ dff renorm(dff a) {
+    const float h = __fadd_rn(a.hi, a.lo);
+    return dff(h, __fsub_rn(a.lo, __fsub_rn(h, a.hi)));
 }
 __host__ __device__ inline dff dff_from(double v) {
     const float h = (float)v;
@@ -65,6 +69,14 @@ template <> __device__ __forceinline__ double2 store_c<double2, cdff>(const cdff
 }
 
 template <class C> __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
+// renormalise a stage result (identity for native types)
+template <class C> __device__ __forceinline__ C cnorm(const C &c) { return c; }
+template <> __device__ __forceinline__ cdff cnorm<cdff>(const cdff &c) {
+    cdff r;
+    r.x = renorm(c.x);
+    r.y = renorm(c.y);
+    return r;
+}
 template <class T, class C> __device__ __forceinline__ void rfma(C &acc, T a, C v) {
     acc.x = tfma(a, v.x, acc.x);
     acc.y = tfma(a, v.y, acc.y);

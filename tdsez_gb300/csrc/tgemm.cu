@@ -5,7 +5,8 @@
 // memory (TMEM, Np <= 256 FP32 columns). K runs in chunks of 32 (one
 // 128-byte swizzled row per operand row) through a two-stage shared-memory
 // pipeline fed by TMA (cp.async.bulk.tensor, 128-byte swizzle):
-//   stage = A (128 x 32 FP32 -> split in place into TF32 hi + lo)
+//   stage = A (128 x 32 FP32 -> split in place into TF32 hi + lo, each
+//           rounded to nearest)
 //         + B hi, B lo (Np x 32 each, precomputed split).
 // Per 8-wide K step the elected thread issues three MMAs,
 //   D += A_hi B_hi + A_hi B_lo + A_lo B_hi,
@@ -114,7 +115,10 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ float tf32_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
+// nearest TF32 value (10 explicit mantissa bits; halfway cases away from zero)
+__device__ __forceinline__ float tf32_round(float v) {
+    return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+}
 
 struct TGParams {
     float *out;
@@ -189,9 +193,10 @@ __global__ void __launch_bounds__(128, 1)
         for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
             const int e = tid + q * 128;
             const float4 v = ah[e];
-            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+            const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
             ah[e] = h;
-            al[e] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+            al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
+                                tf32_round(v.w - h.w));
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -278,11 +283,11 @@ void make_map(CUtensorMap *map, const void *ptr, uint64_t inner, uint64_t outer,
     TDZ_CHECK(r == CUDA_SUCCESS, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
 
-float tf32_trunc_host(double v) {
+float tf32_round_host(double v) {
     float f = (float)v;
     uint32_t u;
     std::memcpy(&u, &f, 4);
-    u &= 0xFFFFE000u;
+    u = (u + 0x1000u) & 0xFFFFE000u;
     std::memcpy(&f, &u, 4);
     return f;
 }
@@ -314,9 +319,9 @@ void TransformMat::build(const std::vector<double> &B, int K_, int N_) {
     for (int n = 0; n < N; ++n)
         for (int k = 0; k < K; ++k) {
             const double v = B[(size_t)k * N + n];
-            const float hi = tf32_trunc_host(v);
+            const float hi = tf32_round_host(v);
             h[(size_t)n * Kp + k] = hi;
-            h[(size_t)(Np + n) * Kp + k] = tf32_trunc_host(v - (double)hi);
+            h[(size_t)(Np + n) * Kp + k] = tf32_round_host(v - (double)hi);
         }
     upload(hilo, h);
     make_map(&map, hilo.ptr, Kp, 2 * (uint64_t)Np, Kp, (uint32_t)Np);

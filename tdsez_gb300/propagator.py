@@ -66,6 +66,12 @@ class Solver:
                                                 C.byref(rn)))
         return its.value, reason.value, rn.value
 
+    def precondition(self, r, z, stream=None):
+        """z = P^-1 r (complex128 CUDA tensors): one preconditioner application."""
+        _lib.check(_lib.load().tdz_solver_precondition(self.handle, C.c_void_p(r.data_ptr()), C.c_void_p(z.data_ptr()),
+                                                       C.c_void_p(_stream(stream))))
+        return z
+
     def __del__(self):
         h = getattr(self, "handle", None)
         if h is not None and h.value:

@@ -1,6 +1,7 @@
 """Tensor-core plane transform (tcgen05, TF32 with a three-term split)
-against numpy FP64, through the C ABI. Bar: 2e-6 relative (max norm), the
-FP32-class accuracy the fast-diagonalisation preconditioner needs."""
+against numpy FP64, through the C ABI. Bar: FP32 class, i.e. a max-norm
+relative error at most 4x that of the same contraction evaluated in FP32 by
+numpy (about 1e-6 at K = 163), and never above 1e-5."""
 import ctypes as C
 
 import numpy as np
@@ -16,6 +17,8 @@ def _run(K, N, planes, R, ldi, ldo, seed):
     x = np.zeros((planes, R, 2, ldi), dtype=np.float32)
     x[..., :K] = rng.standard_normal((planes, R, 2, K)).astype(np.float32)
     ref = np.einsum("prck,kn->pncr", x[..., :K].astype(np.float64), B)
+    ref32 = np.einsum("prck,kn->pncr", x[..., :K], B.astype(np.float32))
+    err32 = np.abs(ref32 - ref).max() / np.abs(ref).max()
     xd = torch.tensor(x.reshape(-1), device="cuda")
     yd = torch.full((planes * N * 2 * ldo,), float("nan"), dtype=torch.float32, device="cuda")
     Bc = np.ascontiguousarray(B)
@@ -23,7 +26,7 @@ def _run(K, N, planes, R, ldi, ldo, seed):
     _lib.check(lib.tdz_plane_transform(Bc.ctypes.data_as(C.POINTER(C.c_double)), K, N, C.c_void_p(xd.data_ptr()),
                                        planes, R, ldi, C.c_void_p(yd.data_ptr()), ldo, C.c_void_p(s)))
     y = yd.cpu().numpy().reshape(planes, N, 2, ldo)[..., :R]
-    return np.abs(y - ref).max() / np.abs(ref).max()
+    return np.abs(y - ref).max() / np.abs(ref).max(), err32
 
 
 @pytest.mark.gpu
@@ -34,8 +37,8 @@ def _run(K, N, planes, R, ldi, ldo, seed):
     (256, 16, 1, 300, 256, 300),      # narrowest N tile, K exactly 8 chunks, 5 M tiles
 ])
 def test_plane_transform(cuda, K, N, planes, R, ldi, ldo):
-    err = _run(K, N, planes, R, ldi, ldo, seed=K + N)
-    assert err < 2e-6, err
+    err, err32 = _run(K, N, planes, R, ldi, ldo, seed=K + N)
+    assert err <= max(4 * err32, 1e-7) and err < 1e-5, (err, err32)
 
 
 @pytest.mark.gpu
@@ -48,4 +51,4 @@ def test_plane_transform_rejects_bad_pitch(cuda):
     y = torch.zeros(64, device="cuda")
     st = lib.tdz_plane_transform(B.ctypes.data_as(C.POINTER(C.c_double)), 6, 6, C.c_void_p(x.data_ptr()), 1, 2, 6,
                                  C.c_void_p(y.data_ptr()), 2, None)
-    assert st == _lib.TDZ_ERR_ARG
+    assert _lib.STATUS_NAMES[st] == "TDZ_ERR_ARG"
