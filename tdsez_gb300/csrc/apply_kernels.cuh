@@ -358,7 +358,12 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
     const size_t smem = rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
     auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
-    if (smem > 48 * 1024) TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // static + dynamic shared memory above 48 KB needs the opt-in (set once per size increase)
+    static size_t opted = 0;
+    if (smem > opted) {
+        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        opted = smem;
+    }
     dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
     kern<<<grid, dim3(txw, kTY3), smem, st>>>(prm);
 }

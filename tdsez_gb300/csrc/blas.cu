@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <type_traits>
 
 #include "cplx.cuh"
 
@@ -54,36 +55,124 @@ __global__ void k_axpbypcz(typename CT<T>::type *y, double ar, double ai, const 
     }
 }
 
-__global__ void k_cast64to32(const double2 *x, float2 *y, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double2 v = x[i];
-        y[i] = make_float2((float)v.x, (float)v.y);
-    }
-}
-
-__global__ void k_cast32to64(const float2 *x, double2 *y, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float2 v = x[i];
-        y[i] = make_double2(v.x, v.y);
-    }
-}
-
-__global__ void k_add_cast(double2 *y, double ar, double ai, const float2 *x, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float2 v = x[i];
-        double2 w = y[i];
-        w.x += ar * v.x - ai * v.y;
-        w.y += ar * v.y + ai * v.x;
-        y[i] = w;
-    }
-}
-
 struct PtrPack {
     const void *p[kMaxDot];
 };
 struct CoefPack {
     double re[kMaxDot], im[kMaxDot];
 };
+
+// ---- FP64 vectors in double-float arithmetic. GB300's FP64 pipe (which also
+// runs FP64 <-> FP32 conversions) issues 2 instructions per clock per SM, so
+// FP64 BLAS written with double arithmetic is bound by that pipe, not by HBM.
+// These kernels split each FP64 element into an FP32 pair with integer
+// operations, compute on the FP32 pipes (about 48 significant bits, relative
+// error near 1e-14) and round back with one FP64 add per component.
+struct CoefDF {
+    dff re[kMaxDot], im[kMaxDot];
+};
+
+inline CoefDF coef_df(const CoefPack &cp, int k) {
+    CoefDF c{};
+    for (int i = 0; i < k; ++i) {
+        c.re[i] = dff_from(cp.re[i]);
+        c.im[i] = dff_from(cp.im[i]);
+    }
+    return c;
+}
+
+__device__ __forceinline__ cdff ld_df(const double2 &v) { return load_c<cdff>(v); }
+__device__ __forceinline__ double2 st_df(const cdff &c) { return store_c<double2>(c); }
+__host__ __device__ inline cdff mk_df(dff re, dff im) {
+    cdff c;
+    c.x = re;
+    c.y = im;
+    return c;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_mdot_df(PtrPack V, const double2 *w, size_t n, double2 *partial) {
+    cdff acc[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) acc[i] = czero<cdff>();
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const cdff wv = ld_df(w[e]);
+#pragma unroll
+        for (int i = 0; i < K; ++i) cfma_conj(acc[i], ld_df(static_cast<const double2 *>(V.p[i])[e]), wv);
+    }
+    __shared__ double2 red[kThreads / 32][K];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        double re = dff_to_double(acc[i].x), im = dff_to_double(acc[i].y);
+        for (int off = 16; off > 0; off >>= 1) {
+            re += __shfl_down_sync(0xffffffffu, re, off);
+            im += __shfl_down_sync(0xffffffffu, im, off);
+        }
+        if (lane == 0) red[warp][i] = make_double2(re, im);
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double re = 0.0, im = 0.0;
+        for (int w2 = 0; w2 < kThreads / 32; ++w2) { re += red[w2][threadIdx.x].x; im += red[w2][threadIdx.x].y; }
+        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_double2(re, im);
+    }
+}
+
+template <int K>
+__global__ void k_maxpy_df(double2 *w, PtrPack V, CoefDF a, size_t n) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        cdff acc = ld_df(w[e]);
+#pragma unroll
+        for (int i = 0; i < K; ++i) cfma(acc, mk_df(a.re[i], a.im[i]), ld_df(static_cast<const double2 *>(V.p[i])[e]));
+        w[e] = st_df(acc);
+    }
+}
+
+// y = a x + b y + c z (zero scalars are skipped; z may be null)
+__global__ void k_axpbypcz_df(double2 *y, cdff a, const double2 *x, cdff b, const double2 *z, cdff c, int use_a,
+                              int use_b, int use_c, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        cdff acc = czero<cdff>();
+        if (use_a) cfma(acc, a, ld_df(x[i]));
+        if (use_b) cfma(acc, b, ld_df(y[i]));
+        if (use_c) cfma(acc, c, ld_df(z[i]));
+        y[i] = st_df(acc);
+    }
+}
+
+__global__ void k_scale_df(double2 *x, cdff a, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        cdff acc = czero<cdff>();
+        cfma(acc, a, ld_df(x[i]));
+        x[i] = st_df(acc);
+    }
+}
+
+__global__ void k_cast64to32_df(const double2 *x, float2 *y, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const cdff v = ld_df(x[i]);
+        y[i] = make_float2(__fadd_rn(v.x.hi, v.x.lo), __fadd_rn(v.y.hi, v.y.lo));
+    }
+}
+
+__global__ void k_cast32to64_df(const float2 *x, double2 *y, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = x[i];
+        y[i] = make_double2(f2d_exact(v.x), f2d_exact(v.y));
+    }
+}
+
+__global__ void k_add_cast_df(double2 *y, cdff a, const float2 *x, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = x[i];
+        cdff acc = ld_df(y[i]);
+        cfma(acc, a, mk_df(dff(v.x), dff(v.y)));
+        y[i] = st_df(acc);
+    }
+}
+
+inline cdff cdf_host(cd a) { return mk_df(dff_from(a.real()), dff_from(a.imag())); }
 
 // per-block partial sums of conj(V_i) w, i < k; partial layout [i][block]
 template <class T, int K>
@@ -161,7 +250,10 @@ __global__ void k_maxpy(typename CT<T>::type *w, PtrPack V, CoefPack a, size_t n
 
 template <class T, int K>
 void mdot_k(const PtrPack &pp, const void *w, size_t n, double2 *partial, int blocks, cudaStream_t st) {
-    k_mdot<T, K><<<blocks, kThreads, 0, st>>>(pp, static_cast<const typename CT<T>::type *>(w), n, partial);
+    if constexpr (std::is_same<T, double>::value)
+        k_mdot_df<K><<<blocks, kThreads, 0, st>>>(pp, static_cast<const double2 *>(w), n, partial);
+    else
+        k_mdot<T, K><<<blocks, kThreads, 0, st>>>(pp, static_cast<const typename CT<T>::type *>(w), n, partial);
 }
 
 template <class T>
@@ -182,7 +274,13 @@ void maxpy_dispatch(int k, void *w, const PtrPack &pp, const CoefPack &cp, size_
     C *wp = static_cast<C *>(w);
     const int g = grid_for(n);
     switch (k) {
-#define TDZ_CASE(K) case K: k_maxpy<T, K><<<g, kThreads, 0, st>>>(wp, pp, cp, n); break;
+#define TDZ_CASE(K)                                                                            \
+    case K:                                                                                    \
+        if constexpr (std::is_same<T, double>::value)                                          \
+            k_maxpy_df<K><<<g, kThreads, 0, st>>>(reinterpret_cast<double2 *>(wp), pp, coef_df(cp, K), n); \
+        else                                                                                   \
+            k_maxpy<T, K><<<g, kThreads, 0, st>>>(wp, pp, cp, n);                              \
+        break;
         TDZ_CASE(1) TDZ_CASE(2) TDZ_CASE(3) TDZ_CASE(4) TDZ_CASE(5) TDZ_CASE(6) TDZ_CASE(7) TDZ_CASE(8)
         TDZ_CASE(9) TDZ_CASE(10) TDZ_CASE(11) TDZ_CASE(12) TDZ_CASE(13) TDZ_CASE(14) TDZ_CASE(15) TDZ_CASE(16)
 #undef TDZ_CASE
@@ -203,7 +301,7 @@ void zero(void *x, size_t n, int prec, cudaStream_t st) {
 
 void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
     const int g = grid_for(n);
-    if (prec == TDZ_FP64) k_scale<double><<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), a.real(), a.imag(), n);
+    if (prec == TDZ_FP64) k_scale_df<<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), cdf_host(a), n);
     else k_scale<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(x), a.real(), a.imag(), n);
     TDZ_CUDA(cudaGetLastError());
     count_launch();
@@ -212,9 +310,9 @@ void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
 void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st) {
     const int g = grid_for(n);
     if (prec == TDZ_FP64)
-        k_axpbypcz<double><<<g, kThreads, 0, st>>>(static_cast<double2 *>(y), a.real(), a.imag(),
-                                                   static_cast<const double2 *>(x), b.real(), b.imag(),
-                                                   static_cast<const double2 *>(z), c.real(), c.imag(), n);
+        k_axpbypcz_df<<<g, kThreads, 0, st>>>(static_cast<double2 *>(y), cdf_host(a), static_cast<const double2 *>(x),
+                                              cdf_host(b), static_cast<const double2 *>(z), cdf_host(c),
+                                              a != 0.0, b != 0.0, z != nullptr && c != 0.0, n);
     else
         k_axpbypcz<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(y), a.real(), a.imag(),
                                                   static_cast<const float2 *>(x), b.real(), b.imag(),
@@ -230,14 +328,15 @@ void axpby(void *y, cd a, const void *x, cd b, size_t n, int prec, cudaStream_t 
 void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st) {
     const int g = grid_for(n);
     if (px == py) { copy(x, y, n, px, st); return; }
-    if (px == TDZ_FP64) k_cast64to32<<<g, kThreads, 0, st>>>(static_cast<const double2 *>(x), static_cast<float2 *>(y), n);
-    else k_cast32to64<<<g, kThreads, 0, st>>>(static_cast<const float2 *>(x), static_cast<double2 *>(y), n);
+    if (px == TDZ_FP64)
+        k_cast64to32_df<<<g, kThreads, 0, st>>>(static_cast<const double2 *>(x), static_cast<float2 *>(y), n);
+    else k_cast32to64_df<<<g, kThreads, 0, st>>>(static_cast<const float2 *>(x), static_cast<double2 *>(y), n);
     TDZ_CUDA(cudaGetLastError());
     count_launch();
 }
 
 void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
-    k_add_cast<<<grid_for(n), kThreads, 0, st>>>(y, a.real(), a.imag(), x, n);
+    k_add_cast_df<<<grid_for(n), kThreads, 0, st>>>(y, cdf_host(a), x, n);
     TDZ_CUDA(cudaGetLastError());
     count_launch();
 }

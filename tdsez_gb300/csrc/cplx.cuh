@@ -48,6 +48,41 @@ __host__ __device__ inline dff dff_from(double v) {
     return dff(h, (float)(v - (double)h));
 }
 
+// FP64 -> double-float split with integer operations only (GB300's FP64 pipe,
+// which also executes FP64 <-> FP32 conversions, issues 2 instructions per
+// clock per SM). hi = v truncated to 24 significant bits, lo = the next 24
+// bits (truncated), so hi + lo carries 48 bits. |v| < 2^-100 (and zero,
+// subnormals) maps to 0; Inf/NaN and |v| >= 2^128 map to a non-finite hi.
+__device__ __forceinline__ dff dff_split(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const unsigned int h32 = (unsigned int)(u >> 32), l32 = (unsigned int)u;
+    const unsigned int sign = h32 & 0x80000000u;
+    const int e = (int)((h32 >> 20) & 0x7FFu) - 1023;
+    if (e < -100) return dff(__uint_as_float(sign), 0.f);
+    if (e > 127) return dff(__uint_as_float(sign | (e == 1024 && ((h32 & 0xFFFFFu) | l32) ? 0x7FC00000u : 0x7F800000u)), 0.f);
+    const unsigned int m23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+    const float hi = __uint_as_float(sign | ((unsigned int)(e + 127) << 23) | m23);
+    const unsigned int m29 = l32 & 0x1FFFFFFFu;
+    if (m29 == 0u) return dff(hi, 0.f);
+    const int lz = __clz((int)m29);                 // >= 3
+    const int el = e - 52 + 31 - lz;                // exponent of the leading remainder bit
+    if (el < -126) return dff(hi, 0.f);
+    const unsigned int frac = (m29 << (lz + 1)) >> 9;
+    return dff(hi, __uint_as_float(sign | ((unsigned int)(el + 127) << 23) | frac));
+}
+// exact FP32 -> FP64 widening with integer operations (normal values; zero and
+// subnormals give signed zero, Inf/NaN stay non-finite)
+__device__ __forceinline__ double f2d_exact(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int ex = (b >> 23) & 0xFFu;
+    unsigned long long d = (unsigned long long)(b & 0x80000000u) << 32;
+    if (ex == 0xFFu) d |= 0x7FF0000000000000ull | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+    else if (ex != 0u) d |= ((unsigned long long)(ex - 127 + 1023) << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)d);
+}
+// hi + lo rounded to FP64: one FP64 add
+__device__ __forceinline__ double dff_to_double(dff a) { return f2d_exact(a.hi) + f2d_exact(a.lo); }
+
 template <class T> struct CT;
 template <> struct CT<float> { using type = float2; };
 template <> struct CT<double> { using type = double2; };
@@ -59,13 +94,13 @@ template <> struct MemC<dff> { using type = double2; };
 template <class C, class M> __device__ __forceinline__ C load_c(const M &m) { return m; }
 template <> __device__ __forceinline__ cdff load_c<cdff, double2>(const double2 &m) {
     cdff c;
-    c.x = dff_from(m.x);
-    c.y = dff_from(m.y);
+    c.x = dff_split(m.x);
+    c.y = dff_split(m.y);
     return c;
 }
 template <class M, class C> __device__ __forceinline__ M store_c(const C &c) { return c; }
 template <> __device__ __forceinline__ double2 store_c<double2, cdff>(const cdff &c) {
-    return make_double2((double)c.x.hi + (double)c.x.lo, (double)c.y.hi + (double)c.y.lo);
+    return make_double2(dff_to_double(c.x), dff_to_double(c.y));
 }
 
 template <class C> __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }

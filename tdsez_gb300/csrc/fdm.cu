@@ -1,8 +1,10 @@
 // Fast-diagonalisation preconditioner (Lynch-Rice-Thomas) for the z-layered
-// operator family: dense eigenvector transforms along x and y (smem-tiled
-// FP32 GEMMs) and one banded complex LU solve per (x, y) line along z with the
-// live stage coefficients. Exact inverse (up to FP32 rounding) when the inner
-// axes carry only mass and stiffness, which is the heterostructure's case.
+// operator family: dense eigenvector transforms along x and y and one banded
+// complex LU solve per (x, y) line along z with the live stage coefficients.
+// Exact inverse (up to FP32 rounding) when the inner axes carry only mass and
+// stiffness, which is the heterostructure's case. 3D with n_x, n_y <= 256:
+// the transforms run on the tensor cores (tgemm.cu) over row-planar FP32
+// buffers; otherwise (2D, wider axes) on the smem-tiled FP32 GEMMs below.
 #include "fdm.h"
 
 #include <cmath>
@@ -218,9 +220,10 @@ __global__ void k_to_planar(const double2 *__restrict__ r, float *__restrict__ a
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t row = e / n0;
         const int x = (int)(e % n0);
-        const double2 v = r[e];
-        a[(row * 2) * ld + x] = (float)v.x;
-        a[(row * 2 + 1) * ld + x] = (float)v.y;
+        const double2 v = r[e];   // FP64 -> FP32 without the (slow) FP64 pipe
+        const dff re = dff_split(v.x), im = dff_split(v.y);
+        a[(row * 2) * ld + x] = __fadd_rn(re.hi, re.lo);
+        a[(row * 2 + 1) * ld + x] = __fadd_rn(im.hi, im.lo);
     }
 }
 
@@ -229,7 +232,7 @@ __global__ void k_from_planar(const float *__restrict__ a, double2 *__restrict__
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t row = e / n0;
         const int x = (int)(e % n0);
-        z[e] = make_double2((double)a[(row * 2) * ld + x], (double)a[(row * 2 + 1) * ld + x]);
+        z[e] = make_double2(f2d_exact(a[(row * 2) * ld + x]), f2d_exact(a[(row * 2 + 1) * ld + x]));
     }
 }
 
