@@ -65,9 +65,12 @@ struct CoefPack {
 // ---- FP64 vectors in double-float arithmetic. GB300's FP64 pipe (which also
 // runs FP64 <-> FP32 conversions) issues 2 instructions per clock per SM, so
 // FP64 BLAS written with double arithmetic is bound by that pipe, not by HBM.
-// These kernels split each FP64 element into an FP32 pair with integer
-// operations, compute on the FP32 pipes (about 48 significant bits, relative
-// error near 1e-14) and round back with one FP64 add per component.
+// The multi-dot and multi-axpy (and complex-scalar updates) split each FP64
+// element into an FP32 pair with integer operations and compute on the FP32
+// pipes (about 48 significant bits, relative error near 1e-14); results that
+// update a stored FP64 vector are added to it in FP64, so the vector keeps
+// its 53 bits. Updates with real scalars (residuals, the CN state update,
+// normalisations) stay in FP64: two FMAs per term and element.
 struct CoefDF {
     dff re[kMaxDot], im[kMaxDot];
 };
@@ -119,13 +122,38 @@ __global__ void __launch_bounds__(kThreads) k_mdot_df(PtrPack V, const double2 *
     }
 }
 
+// w += sum_i a_i V_i: the increment in double-float, the final add in FP64,
+// so w keeps all 53 bits (it is the solution or the Arnoldi vector)
 template <int K>
 __global__ void k_maxpy_df(double2 *w, PtrPack V, CoefDF a, size_t n) {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-        cdff acc = ld_df(w[e]);
+        cdff acc = czero<cdff>();
 #pragma unroll
         for (int i = 0; i < K; ++i) cfma(acc, mk_df(a.re[i], a.im[i]), ld_df(static_cast<const double2 *>(V.p[i])[e]));
-        w[e] = st_df(acc);
+        double2 v = w[e];
+        v.x += dff_to_double(acc.x);
+        v.y += dff_to_double(acc.y);
+        w[e] = v;
+    }
+}
+
+// y = a x + b y + c z with real scalars: native FP64, two FMAs per term and element
+__global__ void k_axpbypcz_r64(double2 *y, double a, const double2 *x, double b, const double2 *z, double c, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        if (a != 0.0) { const double2 v = x[i]; acc.x = a * v.x; acc.y = a * v.y; }
+        if (b != 0.0) { const double2 v = y[i]; acc.x = fma(b, v.x, acc.x); acc.y = fma(b, v.y, acc.y); }
+        if (z && c != 0.0) { const double2 v = z[i]; acc.x = fma(c, v.x, acc.x); acc.y = fma(c, v.y, acc.y); }
+        y[i] = acc;
+    }
+}
+
+__global__ void k_scale_r64(double2 *x, double a, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double2 v = x[i];
+        v.x *= a;
+        v.y *= a;
+        x[i] = v;
     }
 }
 
@@ -301,7 +329,8 @@ void zero(void *x, size_t n, int prec, cudaStream_t st) {
 
 void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
     const int g = grid_for(n);
-    if (prec == TDZ_FP64) k_scale_df<<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), cdf_host(a), n);
+    if (prec == TDZ_FP64 && a.imag() == 0.0) k_scale_r64<<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), a.real(), n);
+    else if (prec == TDZ_FP64) k_scale_df<<<g, kThreads, 0, st>>>(static_cast<double2 *>(x), cdf_host(a), n);
     else k_scale<float><<<g, kThreads, 0, st>>>(static_cast<float2 *>(x), a.real(), a.imag(), n);
     TDZ_CUDA(cudaGetLastError());
     count_launch();
@@ -309,7 +338,10 @@ void scale(void *x, cd a, size_t n, int prec, cudaStream_t st) {
 
 void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st) {
     const int g = grid_for(n);
-    if (prec == TDZ_FP64)
+    if (prec == TDZ_FP64 && a.imag() == 0.0 && b.imag() == 0.0 && c.imag() == 0.0)
+        k_axpbypcz_r64<<<g, kThreads, 0, st>>>(static_cast<double2 *>(y), a.real(), static_cast<const double2 *>(x),
+                                               b.real(), static_cast<const double2 *>(z), c.real(), n);
+    else if (prec == TDZ_FP64)
         k_axpbypcz_df<<<g, kThreads, 0, st>>>(static_cast<double2 *>(y), cdf_host(a), static_cast<const double2 *>(x),
                                               cdf_host(b), static_cast<const double2 *>(z), cdf_host(c),
                                               a != 0.0, b != 0.0, z != nullptr && c != 0.0, n);

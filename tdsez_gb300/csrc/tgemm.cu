@@ -1,25 +1,28 @@
 // tcgen05 transform kernel (see tgemm.h).
 //
-// One CTA of 128 threads computes a 128 x Np output tile (64 complex rows,
-// real and imaginary part rows interleaved) with the accumulator in tensor
-// memory (TMEM, Np <= 256 FP32 columns). K runs in chunks of 32 (one
-// 128-byte swizzled row per operand row) through a two-stage shared-memory
-// pipeline fed by TMA (cp.async.bulk.tensor, 128-byte swizzle):
-//   stage = A (128 x 32 FP32 -> split in place into TF32 hi + lo, each
-//           rounded to nearest)
-//         + B hi, B lo (Np x 32 each, precomputed split).
-// Per 8-wide K step the elected thread issues three MMAs,
+// Persistent CTAs (one per SM, 160 threads) walk 128 x Np output tiles (64
+// complex rows, real and imaginary part rows interleaved); the accumulator
+// lives in tensor memory (TMEM, Np <= 256 FP32 columns). K runs in chunks of
+// 32 (one 128-byte swizzled row per operand row) through an NS-stage ring
+// (NS = 3, or 2 for Np > 192) that warp 4 fills with TMA
+// (cp.async.bulk.tensor, 128-byte swizzle) up to NS chunks ahead, across tile
+// boundaries:
+//   stage = A (128 x 32 FP32, split by warps 0-3 in place into TF32 hi, with
+//           the lo part in one of two extra buffers; both rounded to nearest)
+//         + B hi, B lo (Np x 32 each, split on the host).
+// Per 8-wide K step thread 0 issues three MMAs,
 //   D += A_hi B_hi + A_hi B_lo + A_lo B_hi,
 // which keeps about 22 significant bits (the dropped A_lo B_lo term is
-// ~2^-22 relative), i.e. FP32-class results from TF32 tensor-core rates.
-// The epilogue reads TMEM with tcgen05.ld (warp w owns lanes 32w..32w+31,
-// lane = tile row) and stores the tile transposed per plane.
+// ~2^-22 relative): FP32-class results at TF32 tensor-core rates. At the end
+// of a tile warps 0-3 read TMEM with tcgen05.ld (warp w owns lanes
+// 32w..32w+31, lane = tile row) and store the tile transposed per plane.
 // Every wait on an mbarrier is bounded (clock64): on time-out the kernel sets
-// the error word, skips the remaining MMAs and still frees its TMEM.
+// the error word, the consumers leave together, and TMEM is still freed.
 #include "tgemm.h"
 
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -30,7 +33,6 @@ namespace {
 
 constexpr int TM = 128;        // tile rows (GEMM rows)
 constexpr int KC = 32;         // K per stage (128 bytes of FP32)
-constexpr int NSTAGE = 2;
 constexpr int A_BYTES = TM * KC * 4;   // 16 KB
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
@@ -123,31 +125,61 @@ __device__ __forceinline__ float tf32_round(float v) {
 struct TGParams {
     float *out;
     int rows;      // GEMM rows = 2 planes R
-    int R, N, ldo, nchunks;
+    int R, N, ldo, nchunks, tiles;
 };
 
+// barrier.sync + AND-reduction over `count` threads on named barrier `id`
+__device__ __forceinline__ bool bar_and(int id, int count, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+template <int NP> struct TGShape {
+    static constexpr int B_BYTES = NP * KC * 4;
+    static constexpr int STAGE = A_BYTES + 2 * B_BYTES;          // A (FP32 -> TF32 hi in place), B hi, B lo
+    static constexpr int NS = 3 * STAGE + 2 * A_BYTES + 1100 <= 232448 ? 3 : 2;
+    static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 2 * A_BYTES + 2 * NS * 8 + 16;
+};
+
+// Persistent, warp-specialised: warps 0-3 split A, issue the MMAs (thread 0)
+// and run the epilogue; warp 4 (one lane) is the TMA producer, running up to
+// NS chunks ahead across tile boundaries, so loads overlap the epilogue.
 template <int NP>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(160, 1)
     k_transform(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap, const TGParams prm) {
-    constexpr int B_BYTES = NP * KC * 4;
-    constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    using S = TGShape<NP>;
+    constexpr int NS = S::NS, STAGE = S::STAGE, B_BYTES = S::B_BYTES;
     constexpr uint32_t TMEM_COLS = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;
     static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N tile");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base + NSTAGE * STAGE);   // full[2], done[2]
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NSTAGE);
+    uint8_t *alo_base = base + NS * STAGE;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(alo_base + 2 * A_BYTES);   // full[NS], done[NS]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * TM;
     const int nch = prm.nchunks;
-    auto a_hi = [&](int s) { return base + s * STAGE; };
-    auto a_lo = [&](int s) { return base + s * STAGE + A_BYTES; };
-    auto b_hi = [&](int s) { return base + s * STAGE + 2 * A_BYTES; };
-    auto b_lo = [&](int s) { return base + s * STAGE + 2 * A_BYTES + B_BYTES; };
-    const uint32_t full0 = smem_u32(&bars[0]), done0 = smem_u32(&bars[NSTAGE]);
+    const int my_tiles = prm.tiles > (int)blockIdx.x ? (prm.tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int G = my_tiles * nch;
+    auto a_st = [&](int s) { return base + s * STAGE; };
+    auto bh_st = [&](int s) { return base + s * STAGE + A_BYTES; };
+    auto bl_st = [&](int s) { return base + s * STAGE + A_BYTES + B_BYTES; };
+    auto a_lo = [&](int g) { return alo_base + (g & 1) * A_BYTES; };
+    const uint32_t full0 = smem_u32(&bars[0]), done0 = smem_u32(&bars[NS]);
 
     if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(done0 + 8 * s, 1);
         }
@@ -163,87 +195,93 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = instr_desc(NP);
-    constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
-    bool ok = true;
 
-    auto issue = [&](int c, int s) {
-        mbar_expect_tx(full0 + 8 * s, TX);
-        tma_load_2d(smem_u32(a_hi(s)), &amap, c * KC, m0, full0 + 8 * s);
-        tma_load_2d(smem_u32(b_hi(s)), &bmap, c * KC, 0, full0 + 8 * s);
-        tma_load_2d(smem_u32(b_lo(s)), &bmap, c * KC, NP, full0 + 8 * s);
-    };
-    if (tid == 0) issue(0, 0);
-    for (int c = 0; c < nch; ++c) {
-        const int s = c & 1;
-        if (tid == 0 && c + 1 < nch) {
-            const int s1 = (c + 1) & 1;
-            if (c >= 1) ok = ok && mbar_wait(done0 + 8 * s1, ((c - 1) >> 1) & 1);
-            if (ok) issue(c + 1, s1);
-        }
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        if (!mbar_wait(full0 + 8 * s, (c >> 1) & 1)) ok = false;
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        // split A into TF32 hi (in place) and lo
-        float4 *ah = reinterpret_cast<float4 *>(a_hi(s));
-        float4 *al = reinterpret_cast<float4 *>(a_lo(s));
-#pragma unroll
-        for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
-            const int e = tid + q * 128;
-            const float4 v = ah[e];
-            const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
-            ah[e] = h;
-            al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
-                                tf32_round(v.w - h.w));
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t ah_a = smem_u32(a_hi(s)), al_a = smem_u32(a_lo(s));
-            const uint32_t bh_a = smem_u32(b_hi(s)), bl_a = smem_u32(b_lo(s));
-#pragma unroll
-            for (int j = 0; j < KC / 8; ++j) {
-                const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the swizzled row
-                const uint64_t dah = smem_desc(ah_a + off), dal = smem_desc(al_a + off);
-                const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
-                mma_tf32(tmem, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
-                mma_tf32(tmem, dah, dbl, idesc, 1u);
-                mma_tf32(tmem, dal, dbh, idesc, 1u);
+    if (warp == 4) {
+        // ---- producer
+        if (lane == 0) {
+            constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
+            for (int g = 0; g < G; ++g) {
+                const int s = g % NS;
+                if (g >= NS && !mbar_wait(done0 + 8 * s, ((g - NS) / NS) & 1)) break;
+                const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x, c = g % nch;
+                mbar_expect_tx(full0 + 8 * s, TX);
+                tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TM, full0 + 8 * s);
+                tma_load_2d(smem_u32(bh_st(s)), &bmap, c * KC, 0, full0 + 8 * s);
+                tma_load_2d(smem_u32(bl_st(s)), &bmap, c * KC, NP, full0 + 8 * s);
             }
-            mma_commit(done0 + 8 * s);
         }
-    }
-    // all MMAs done: the last commit covers every earlier MMA of the thread
-    if (ok) ok = mbar_wait(done0 + 8 * ((nch - 1) & 1), ((nch - 1) >> 1) & 1);
-    ok = __syncthreads_and(ok) != 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-        const int g = m0 + warp * 32 + lane;   // this thread's tile row
-        const bool row_ok = g < prm.rows;
-        const int cr = g >> 1, part = g & 1;
-        const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
-        float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
-        const size_t nstride = (size_t)2 * prm.ldo;
-#pragma unroll 1
-        for (int c0 = 0; c0 < NP; c0 += 16) {
-            uint32_t v[16];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row_ok) {
+    } else {
+        // ---- consumers: 128 threads, named barrier 1
+        const uint32_t idesc = instr_desc(NP);
+        for (int g = 0; g < G; ++g) {
+            const int s = g % NS, c = g % nch;
+            bool ok = mbar_wait(full0 + 8 * s, (g / NS) & 1);
+            if (ok && g >= 2) ok = mbar_wait(done0 + 8 * ((g - 2) % NS), ((g - 2) / NS) & 1);   // A_lo[g & 1] free
+            if (!bar_and(1, 128, ok)) break;
+            // split A into TF32 hi (in place) and lo, both rounded to nearest
+            float4 *ah = reinterpret_cast<float4 *>(a_st(s));
+            float4 *al = reinterpret_cast<float4 *>(a_lo(g));
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int n = c0 + j;
-                    if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+            for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
+                const int e = tid + q * 128;
+                const float4 v = ah[e];
+                const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+                ah[e] = h;
+                al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
+                                    tf32_round(v.w - h.w));
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bar_sync(1, 128);
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t ah_a = smem_u32(a_st(s)), al_a = smem_u32(a_lo(g));
+                const uint32_t bh_a = smem_u32(bh_st(s)), bl_a = smem_u32(bl_st(s));
+#pragma unroll
+                for (int j = 0; j < KC / 8; ++j) {
+                    const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the swizzled row
+                    const uint64_t dah = smem_desc(ah_a + off), dal = smem_desc(al_a + off);
+                    const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
+                    mma_tf32(tmem, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                    mma_tf32(tmem, dah, dbl, idesc, 1u);
+                    mma_tf32(tmem, dal, dbh, idesc, 1u);
                 }
+                mma_commit(done0 + 8 * s);
+            }
+            if (c == nch - 1) {
+                // tile complete: TMEM -> registers -> global (transposed per plane)
+                const bool okd = mbar_wait(done0 + 8 * s, (g / NS) & 1);
+                if (!bar_and(1, 128, okd)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x;
+                const int row = tile * TM + warp * 32 + lane;
+                const bool row_ok = row < prm.rows;
+                const int cr = row >> 1, part = row & 1;
+                const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
+                float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
+                const size_t nstride = (size_t)2 * prm.ldo;
+#pragma unroll 1
+                for (int c0 = 0; c0 < NP; c0 += 16) {
+                    uint32_t v[16];
+                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (row_ok) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int n = c0 + j;
+                            if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+                        }
+                    }
+                }
+                // the next tile's first MMA overwrites the accumulator
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                bar_sync(1, 128);
             }
         }
     }
@@ -292,16 +330,25 @@ float tf32_round_host(double v) {
     return f;
 }
 
-template <int NP> void launch(const TransformMat &T, const CUtensorMap &amap, const TGParams &prm, int tiles,
-                              cudaStream_t st) {
-    constexpr int STAGE = 2 * A_BYTES + 2 * NP * KC * 4;
-    const size_t smem = 1024 + (size_t)NSTAGE * STAGE + 2 * NSTAGE * 8 + 16;
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        TDZ_CUDA(cudaGetDevice(&dev));
+        TDZ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return n;
+}
+
+template <int NP> void launch(const TransformMat &T, const CUtensorMap &amap, const TGParams &prm, cudaStream_t st) {
+    const size_t smem = TGShape<NP>::SMEM;
     static bool attr = false;   // set once per process (same device attribute for every device)
     if (!attr) {
         TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    k_transform<NP><<<tiles, 128, smem, st>>>(amap, T.map, prm);
+    const int grid = std::min(prm.tiles, sm_count());
+    k_transform<NP><<<grid, 160, smem, st>>>(amap, T.map, prm);
 }
 
 }  // namespace
@@ -351,24 +398,24 @@ void transform(const TransformMat &T, const float *in, int planes, int R, int ld
     prm.N = T.N;
     prm.ldo = ldo;
     prm.nchunks = T.Kp / KC;
-    const int tiles = (int)((rows + TM - 1) / TM);
+    prm.tiles = (int)((rows + TM - 1) / TM);
     switch (T.Np) {
-    case 16: launch<16>(T, amap, prm, tiles, st); break;
-    case 32: launch<32>(T, amap, prm, tiles, st); break;
-    case 48: launch<48>(T, amap, prm, tiles, st); break;
-    case 64: launch<64>(T, amap, prm, tiles, st); break;
-    case 80: launch<80>(T, amap, prm, tiles, st); break;
-    case 96: launch<96>(T, amap, prm, tiles, st); break;
-    case 112: launch<112>(T, amap, prm, tiles, st); break;
-    case 128: launch<128>(T, amap, prm, tiles, st); break;
-    case 144: launch<144>(T, amap, prm, tiles, st); break;
-    case 160: launch<160>(T, amap, prm, tiles, st); break;
-    case 176: launch<176>(T, amap, prm, tiles, st); break;
-    case 192: launch<192>(T, amap, prm, tiles, st); break;
-    case 208: launch<208>(T, amap, prm, tiles, st); break;
-    case 224: launch<224>(T, amap, prm, tiles, st); break;
-    case 240: launch<240>(T, amap, prm, tiles, st); break;
-    case 256: launch<256>(T, amap, prm, tiles, st); break;
+    case 16: launch<16>(T, amap, prm, st); break;
+    case 32: launch<32>(T, amap, prm, st); break;
+    case 48: launch<48>(T, amap, prm, st); break;
+    case 64: launch<64>(T, amap, prm, st); break;
+    case 80: launch<80>(T, amap, prm, st); break;
+    case 96: launch<96>(T, amap, prm, st); break;
+    case 112: launch<112>(T, amap, prm, st); break;
+    case 128: launch<128>(T, amap, prm, st); break;
+    case 144: launch<144>(T, amap, prm, st); break;
+    case 160: launch<160>(T, amap, prm, st); break;
+    case 176: launch<176>(T, amap, prm, st); break;
+    case 192: launch<192>(T, amap, prm, st); break;
+    case 208: launch<208>(T, amap, prm, st); break;
+    case 224: launch<224>(T, amap, prm, st); break;
+    case 240: launch<240>(T, amap, prm, st); break;
+    case 256: launch<256>(T, amap, prm, st); break;
     default: throw Error(TDZ_ERR_INTERNAL, "bad transform tile width");
     }
     TDZ_CUDA(cudaGetLastError());
