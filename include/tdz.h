@@ -101,6 +101,12 @@ typedef struct tdz_physics {
     double cap_inv_mass;        /* 1/m scale of the CAP (TDSEZCapMassScale)     */
     int coupled[3];             /* 1 = field couples on this axis (dipole term) */
     int dirichlet;              /* 1 = homogeneous Dirichlet walls (1D only)    */
+    int nsoft;                  /* soft-core centres (2D/3D, at most 8)         */
+    const double *soft;         /* nsoft x 5: Z, cx, cy, cz, a; adds the non-
+                                   separable V(r) = -Z / sqrt(|r - c|^2 + a),
+                                   e.g. V = -1/sqrt(x^2+y^2+1), applied by
+                                   per-element quadrature (TDSEZFormHam,
+                                   src/assembly/assembly.cpp:703-864)        */
 } tdz_physics;
 
 /* ------------------------------------------------------------- operator

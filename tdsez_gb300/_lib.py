@@ -36,6 +36,8 @@ class tdz_physics(C.Structure):
         ("cap_inv_mass", C.c_double),
         ("coupled", C.c_int * 3),
         ("dirichlet", C.c_int),
+        ("nsoft", C.c_int),
+        ("soft", C.POINTER(C.c_double)),
     ]
 
 

@@ -327,12 +327,26 @@ __global__ void k_apply1d(const ApplyParams<T> prm) {
 constexpr int kTX3 = 32, kTY3 = 8, kTX2 = 128;
 
 // z chunk per CTA: about `target` CTAs in total, chunks no shorter than 4p
-// planes (the 2p halo planes of a chunk are re-read and, in the compute-bound
-// double-float kernel, recomputed)
+// planes (the 2p halo planes of a chunk are re-read)
 inline int pick_chunk(int tiles, int n_outer, int P, int target = 152 * 8) {
     int chunks = (target + tiles - 1) / tiles;
     chunks = std::max(1, std::min(chunks, n_outer / std::max(1, 4 * P)));
     return (n_outer + chunks - 1) / chunks;
+}
+
+// compute-bound kernels: the chunk count that minimises waves x (chunk + 2p),
+// i.e. the time of the slowest SM including the halo planes each chunk
+// recomputes, for `slots` resident CTAs on the GPU
+inline int pick_chunk_waves(int tiles, int n_outer, int P, int slots) {
+    int best = n_outer;
+    double best_t = 1e300;
+    for (int c = 1; c <= std::max(1, n_outer / std::max(1, 4 * P)); ++c) {
+        const int len = (n_outer + c - 1) / c;
+        const long long ctas = (long long)tiles * ((n_outer + len - 1) / len);
+        const double t = (double)((ctas + slots - 1) / slots) * (len + 2 * P);
+        if (t < best_t - 1e-9) { best_t = t; best = len; }
+    }
+    return best;
 }
 
 // tile width 16..32 (multiple of 4) with the least padding of n0; ties go to the wider
@@ -349,15 +363,31 @@ template <class T, int P, bool HB, bool HC>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     using C = typename CT<T>::type;
     ApplyParams<T> prm = prm0;
-    const int txw = pick_tile_x(prm.n0);
+    auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
+    // FP32 (HBM-leaning): full warps along x, about 8 CTAs per SM. FP64 and
+    // double-float (FP64/FP32-pipe bound): the tile width with the least x
+    // padding and the z chunking with the fewest waves x (chunk + halo).
+    const bool fp32 = std::is_same<T, float>::value;
+    const int txw = fp32 ? kTX3 : pick_tile_x(prm.n0);
     const int tiles = ((prm.n0 + txw - 1) / txw) * ((prm.n1 + kTY3 - 1) / kTY3);
-    // compute-bound double-float: about two waves of two CTAs per SM; otherwise about 8 CTAs per SM
-    const int target = std::is_same<T, float>::value ? 152 * 8 : 152 * 4;
-    prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P, target), 96);
+    if (fp32) {
+        prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P), 96);
+    } else {
+        static int slots = 0;   // resident CTAs on the GPU at the largest dynamic smem (96-plane chunks)
+        if (!slots) {
+            const size_t smax = (size_t)(96 + 2 * P) * (2 * P + 1) * (sizeof(C) * (HC ? 2 : 1) + (HB ? sizeof(T) : 0));
+            TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+            int per_sm = 0, dev = 0, nsm = 0;
+            TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, txw * kTY3, smax));
+            TDZ_CUDA(cudaGetDevice(&dev));
+            TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            slots = std::max(1, per_sm) * nsm;
+        }
+        prm.zchunk = std::min(pick_chunk_waves(tiles, prm.n2, P, slots), 96);
+    }
     prm.zchunk_planes = prm.zchunk + 2 * P;
     const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
     const size_t smem = rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
-    auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
     // static + dynamic shared memory above 48 KB needs the opt-in (set once per size increase)
     static size_t opted = 0;
     if (smem > opted) {

@@ -17,7 +17,7 @@ namespace blas {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRedBlocks = 2 * 152;
+constexpr int kRedBlocks = 8 * 152;   // about 8 CTAs per SM: latency hiding for the double-float dots
 
 inline int grid_for(size_t n) {
     const size_t b = (n + kThreads - 1) / kThreads;

@@ -421,6 +421,7 @@ void PcFDM::setup(Operator *op_) {
         return true;
     };
     if (pl.hasB && (!pure_s(pl.xT) || (dim == 3 && !pure_s(pl.yT)))) exact = false;
+    if (op->quad.on) exact = false;   // the non-separable term is left out of the fast inverse
     for (int d = 0; d < 3; ++d) n[d] = d < dim ? s.ax[d].n : 1;
     N = (size_t)s.ndof();
     tensor = dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);

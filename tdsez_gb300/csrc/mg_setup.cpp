@@ -179,7 +179,9 @@ void Multigrid::setup(Operator *fine_, const MGOptions &o, cudaStream_t st) {
             m.space.nquad = fs.nquad;
             for (int d = 0; d < dim; ++d) {
                 const auto &U = K[l][d];
-                m.space.ax[d].setup(U.data(), (int)U.size(), p, std::max(1, std::min(fs.nquad, 2)));
+                // a level carrying the soft-core term needs the full Gauss rule for its quadrature
+                const int nq = fine->quad.on ? fs.nquad : std::max(1, std::min(fs.nquad, 2));
+                m.space.ax[d].setup(U.data(), (int)U.size(), p, nq);
             }
             // Galerkin operator from the next finer level
             const Operator &fo = *lv[l - 1].opp;
@@ -200,6 +202,9 @@ void Multigrid::setup(Operator *fine_, const MGOptions &o, cudaStream_t st) {
                 for (const BandD &b : fo.bases[d]) op->bases[d].push_back(galerkin(m.P[d], b));
             }
             op->upload_bases();
+            // the non-separable term is rediscretised on the level (its Galerkin
+            // product is not a Kronecker sum)
+            if (fo.quad.on) op->quad.build(op->space, fo.quad.nsoft, &fo.quad.soft[0][0]);
             m.opp = op.get();
             m.op = std::move(op);
         }

@@ -139,6 +139,9 @@ void Operator::build(const Space &s, const tdz_physics &ph) {
             m_wall[slot] += mD;
         }
     }
+    // non-separable soft-core centres: per-element quadrature term of H
+    quad.build(s, ph.nsoft, ph.soft);
+    phys.soft = nullptr;   // the caller's array is not kept
     sigma = {cd(1.0), cd(0.0), cd(0.0), cd(0.0), cd(0.0)};
     upload_bases();
 }
@@ -262,6 +265,11 @@ void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t s
     if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");
     Plan &pl = plan(which);
     launch_apply(*this, pl, prec, x, y, st);
+    if (quad.on && (which == TDZ_HAMILTONIAN || which == TDZ_STAGE)) {
+        // y += s (g for the stage) V_q x
+        const cd coef = -phys.charge * (which == TDZ_STAGE ? sigma[1] : cd(1.0));
+        quad.apply(coef, prec, x, y, st);
+    }
     ++launches;
 }
 

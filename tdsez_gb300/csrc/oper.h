@@ -7,6 +7,7 @@
 #include <memory>
 #include <vector>
 
+#include "quad.h"
 #include "space.h"
 
 namespace tdz {
@@ -56,6 +57,7 @@ struct Operator {
     std::vector<Term> terms;                    // all terms of the stage operator
     std::vector<int> coupled;                   // coupled axes in order
     double cap_bound = 0.0;                     // bound on the CAP part of M^-1 H (Rayleigh quotient)
+    QuadTerm quad;                              // non-separable soft-core potential (per-element quadrature)
     // 1D Dirichlet walls: wall diagonal of H and M
     bool wall1d = false;
     double h_wall[2] = {0, 0}, m_wall[2] = {0, 0};

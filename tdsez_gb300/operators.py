@@ -64,6 +64,8 @@ class Physics:
     bounds: Sequence[tuple] = ()
     coupled: Sequence[int] = (0,)
     dirichlet: bool = False
+    # non-separable soft-core centres (Z, cx, cy, cz, a): V(r) += -Z / sqrt(|r - c|^2 + a)
+    softcore: Sequence[tuple] = ()
 
     @property
     def sign(self) -> float:
@@ -109,6 +111,12 @@ class Operator:
             if a < space.dim:
                 st.coupled[a] = 1
         st.dirichlet = 1 if phys.dirichlet else 0
+        if phys.softcore:
+            arr = np.ascontiguousarray(np.array([list(c) + [0.0] * (5 - len(c)) if len(c) < 5 else list(c)
+                                                 for c in phys.softcore], dtype=np.float64).reshape(-1))
+            self._keep.append(arr)
+            st.nsoft = len(phys.softcore)
+            st.soft = _lib.dptr(arr)
         self.coupled = [a for a in range(space.dim) if st.coupled[a]]
         h = C.c_void_p()
         _lib.check(lib.tdz_operator_create(space.handle, C.byref(st), C.byref(h)))

@@ -94,17 +94,59 @@ def _c7():
     return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, V=V, coupled=(0, 1, 2))
 
 
+@case("2d_softcore")
+def _c8():
+    """The 2D soft-core Coulomb carrier of the 512^2 Pade(2,2) configuration,
+    V = -1/sqrt(x^2 + y^2 + 1), with CAP and a field along x (small grid)."""
+    p, nq = 4, 5
+    knots = [ob.uniform_knots(14, -20.0, 20.0, p), ob.uniform_knots(13, -20.0, 20.0, p)]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, coupled=(0,), cap_kmin=1.0,
+                bounds=[(-20.0, 20.0), (-20.0, 20.0)], soft=[(1.0, 0.0, 0.0, 0.0, 1.0)])
+
+
+@case("3d_softcore")
+def _c9():
+    """The 3D soft-core carrier of the 192^3 Magnus-4 configuration,
+    V = -1/sqrt(r^2 + 0.5), symmetric exponential knots with a knot at 0,
+    field along z (small grid)."""
+    p, nq = 4, 5
+    knots = [ob.symexp_knots(-12.0, 12.0, 6, 0.9, p)] * 3
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, coupled=(2,), soft=[(1.0, 0.0, 0.0, 0.0, 0.5)])
+
+
+@case("3d_two_centres_p3")
+def _c10():
+    """Two soft-core centres off the grid axes plus a separable confinement, p = 3."""
+    p, nq = 3, 4
+    knots = [ob.uniform_knots(7, -9.0, 9.0, p), ob.uniform_knots(6, -8.0, 8.0, p), ob.uniform_knots(8, -10.0, 10.0, p)]
+    V = [lambda x: 0.005 * x * x, None, None]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, V=V, coupled=(0, 1, 2),
+                soft=[(0.5, -1.0, 0.0, 0.0, 1.0), (0.7, 1.0, 0.5, -0.5, 0.8)])
+
+
+def _soft_value(soft, r):
+    v = 0.0
+    for Z, cx, cy, cz, a in soft:
+        d = (r[0] - cx, r[1] - cy, r[2] - cz)
+        v -= Z / np.sqrt(d[0] ** 2 + d[1] ** 2 + d[2] ** 2 + a)
+    return v
+
+
 def oracle_of(c):
     """Oracle Space, Physics, Assembled for a case dict."""
     axes = [ob.Axis(k, c["p"], c["nq"]) for k in c["knots"]]
     S = ob.Space(axes)
     dim = S.dim
     Vs = list(c.get("V", [None] * dim)) + [None] * 3
-    have_v = any(v is not None for v in Vs[:dim])
+    soft = c.get("soft", [])
+    have_v = any(v is not None for v in Vs[:dim]) or bool(soft)
 
     def pot(x, y, z):
         r = (x, y, z)
-        return sum(Vs[d](r[d]) for d in range(dim) if Vs[d] is not None)
+        v = sum(Vs[d](r[d]) for d in range(dim) if Vs[d] is not None)
+        if soft:   # 2D cases: the centres' z offset is irrelevant (r_z = 0, c_z = 0)
+            v += _soft_value(soft, (x, y if dim > 1 else 0.0, z if dim > 2 else 0.0))
+        return v
     ma = c.get("mass_axis")
     if ma is None:
         ph = oo.Physics(dim=dim, charge=c["charge"], potential=pot if have_v else None,
@@ -131,5 +173,6 @@ def product_of(c):
     dim = S.dim
     ph = Physics(charge=c["charge"], mass=c.get("mass", 1.0), mass_axis=c.get("mass_axis"),
                  inv_mass_fn=c.get("inv_mass"), potential=list(c.get("V", [])), cap_kmin=c.get("cap_kmin"),
-                 bounds=c.get("bounds", ()), coupled=c["coupled"], dirichlet=c.get("dirichlet", False))
+                 bounds=c.get("bounds", ()), coupled=c["coupled"], dirichlet=c.get("dirichlet", False),
+                 softcore=c.get("soft", ()))
     return S, Operator(S, ph)

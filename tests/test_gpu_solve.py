@@ -22,7 +22,8 @@ def _berr(Am, x, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_const_mass_cap", "2d_cap_softcore_sep", "3d_p2_hole"])
+@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_const_mass_cap", "2d_cap_softcore_sep", "3d_p2_hole",
+                                  "3d_softcore"])
 @pytest.mark.parametrize("pc,prec,outer", [("mg", "fp32", "fp64"), ("mg", "fp64", "fp64"), ("mass", "fp32", "fp64"),
                                            ("mass", "fp64", "fp64"), ("mg", "fp32", "df")])
 def test_stage_solve_parity(cuda, name, pc, prec, outer):
@@ -56,7 +57,8 @@ def test_stage_solve_parity(cuda, name, pc, prec, outer):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_p2_hole", "3d_p5_sym", "2d_cap_softcore_sep"])
+@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_p2_hole", "3d_p5_sym", "2d_cap_softcore_sep",
+                                  "3d_softcore"])
 def test_fdm_solve(cuda, name):
     """Fast-diagonalisation preconditioner: exact (FP32) for operators whose
     inner axes carry only mass and stiffness (heterostructure), approximate
@@ -84,7 +86,8 @@ def test_fdm_solve(cuda, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["3d_heterostructure", "2d_cap_softcore_sep", "3d_const_mass_cap"])
+@pytest.mark.parametrize("name", ["3d_heterostructure", "2d_cap_softcore_sep", "3d_const_mass_cap", "2d_softcore",
+                                  "3d_two_centres_p3"])
 @pytest.mark.parametrize("kind", ["cn", "pade22", "magnus4"])
 def test_propagation_parity(cuda, name, kind):
     """Several steps with a time-dependent field: GPU state == oracle state."""
