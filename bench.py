@@ -261,13 +261,22 @@ def run_tdz(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
                 "steps": ke},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "fused stage apply, FP32 (multigrid smoother and residual)", "bound": "hbm",
-                     "achieved": ach32, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": ach32 / pk.get("hbm_gbs", 6800.0), "traffic": None,
-                     "launch_us": t32 * 1e6, "bytes_per_launch": bytes32,
-                     "fp64_apply": {"achieved": ach64, "launch_us": t64 * 1e6, "bytes_per_launch": bytes64},
-                     "df_apply": {"achieved": bytes64 / tdf / 1e9, "launch_us": tdf * 1e6,
-                                  "bytes_per_launch": bytes64}},
+        # dominant kernel of the CN step (about half of it): the double-float stage apply on FP64
+        # vectors, 32 algorithmic bytes per coefficient (x read, y written once). It is bound by the
+        # FP32 pipes (double-float arithmetic), so its HBM fraction is low by construction; traffic is
+        # dram read + write of one launch from the ncu capture in profiles/.
+        "roofline": {"kernel": "k_apply3d<dff> double-float stage apply (FGMRES residual and Arnoldi)",
+                     "bound": "hbm", "achieved": bytes64 / tdf / 1e9, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": bytes64 / tdf / 1e9 / pk.get("hbm_gbs", 6800.0), "traffic": DF_APPLY_TRAFFIC,
+                     "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+                     "launch_us": tdf * 1e6, "bytes_per_launch": bytes64,
+                     "limiter": "FP32 pipes: 12 FP32 instructions per double-float FMA (ncu: 50.6% issue, "
+                                "42.8% FMA pipe)",
+                     "fp32_apply": {"kernel": "k_apply3d<float> (multigrid smoother and residual)",
+                                    "achieved": ach32, "frac": ach32 / pk.get("hbm_gbs", 6800.0),
+                                    "launch_us": t32 * 1e6, "bytes_per_launch": bytes32},
+                     "fp64_apply": {"kernel": "k_apply3d<double> (native FP64, not used by the step)",
+                                    "achieved": ach64, "launch_us": t64 * 1e6, "bytes_per_launch": bytes64}},
         "clocks": clk.summary(),
         "setup_s": t_setup,
     }
@@ -281,6 +290,9 @@ def run_tdz(args):
 
 
 CPU_GRID = (16, 16, 32)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_apply3d<dff,3,0,1> launch on the
+# 160x160x320 workload (ncu --set full, profiles/k_apply3d_df_stage_heterostructure_160x160x320_p3.md)
+DF_APPLY_TRAFFIC = 146.86e6 + 99.14e6
 
 
 def apply_only(args, op, S, psi0, stream):

@@ -165,6 +165,9 @@ typedef struct tdz_solver_opts {
     int outer_precision;/* operator applies of the FP64 Krylov method and the
                            step right-hand sides: TDZ_FP64 (also 0) or
                            TDZ_FP64_DF                                        */
+    int mg_learned;     /* 1 = learned CNN correction of the coarsest solve
+                           (TDZ_PC_MG with FP32 levels; active once trained by
+                           tdz_solver_train_coarse)                          */
 } tdz_solver_opts;
 /* Set up the solver for the current stage of op (call set_stage first). */
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);
@@ -178,6 +181,22 @@ tdz_status tdz_solver_solve(tdz_solver *s, const void *b, void *x, void *stream,
  * adapter (the PCMG V-cycle of src/multigrid.cpp:275-325). */
 tdz_status tdz_solver_precondition(tdz_solver *s, const void *r, void *z, void *stream);
 void tdz_solver_destroy(tdz_solver *s);
+
+/* Train the learned coarse correction of a TDZ_PC_MG solver created with
+ * mg_learned = 1, for the operator's current stage: `pairs` (residual, error)
+ * pairs generated at the coarsest level by the solver itself (random coarse
+ * right-hand sides, the production Chebyshev coarse solve, a 10x longer
+ * solve for the error), then `epochs` passes of Adam (learning rate lr,
+ * batches of 8) with the hand-written CNN kernels. *loss (may be NULL): mean
+ * relative squared error of the last epoch. No counterpart in the reference
+ * (whose coarse solve is a MUMPS LU, src/multigrid.cpp:315-324). */
+tdz_status tdz_solver_train_coarse(tdz_solver *s, int pairs, int epochs, float lr, unsigned long long seed,
+                                   float *loss, void *stream);
+/* Relative error of the coarsest-level solve against a 10x longer solve on
+ * `trials` random right-hand sides, without (*plain) and with (*learned) the
+ * trained network: what the network gains at its own task. */
+tdz_status tdz_solver_coarse_gain(tdz_solver *s, int trials, unsigned long long seed, double *plain,
+                                  double *learned, void *stream);
 
 /* out = sum_i conj(x_i) y_i over n complex coefficients (FP32 or FP64 device
  * vectors), accumulated in FP64 by a deterministic two-pass reduction (the

@@ -52,6 +52,7 @@ class tdz_solver_opts(C.Structure):
         ("mg_smooth", C.c_int),
         ("mg_coarse_its", C.c_int),
         ("outer_precision", C.c_int),
+        ("mg_learned", C.c_int),
     ]
 
 
@@ -116,6 +117,8 @@ SIGNATURES = {
     "tdz_tsurff_amplitudes": (I, [VP, C.POINTER(D), VP]),
     "tdz_tsurff_volkov": (I, [VP, C.POINTER(D)]),
     "tdz_tsurff_destroy": (None, [VP]),
+    "tdz_solver_train_coarse": (I, [VP, I, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), VP]),
+    "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
     "tdz_plane_transform": (I, [C.POINTER(C.c_double), I, I, VP, I, I, I, VP, I, VP]),
     "tdz_cnn_create": (I, [I, I, I, I, I, I, I, I, C.c_ulonglong, PP]),
     "tdz_cnn_forward": (I, [VP, VP, VP, I, VP]),

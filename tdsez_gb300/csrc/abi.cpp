@@ -257,6 +257,7 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     so.mg.smooth = o->mg_smooth > 0 ? o->mg_smooth : 8;
     so.mg.coarse_its = o->mg_coarse_its > 0 ? o->mg_coarse_its : 12;
     so.outer = o->outer_precision == 0 ? TDZ_FP64 : o->outer_precision;
+    so.mg.learned = o->mg_learned;
     TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
               "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;
@@ -297,6 +298,35 @@ tdz_status tdz_solver_solve(tdz_solver *s, const void *b, void *x, void *stream,
         if (its) *its = st.its;
         if (reason) *reason = st.reason;
         if (rnorm) *rnorm = st.rnorm;
+    });
+}
+
+static tdz::Multigrid *learned_mg(tdz_solver *s) {
+    TDZ_CHECK(s, TDZ_ERR_ARG, "null solver");
+    TDZ_CHECK(s->s.opt.pc == TDZ_PC_MG, TDZ_ERR_STATE, "the learned coarse correction needs TDZ_PC_MG");
+    auto *mg = static_cast<tdz::Multigrid *>(s->s.pc.get());
+    TDZ_CHECK(mg->lrn.on, TDZ_ERR_STATE, "solver created without mg_learned (or with FP64 levels)");
+    return mg;
+}
+
+tdz_status tdz_solver_train_coarse(tdz_solver *s, int pairs, int epochs, float lr, unsigned long long seed,
+                                   float *loss, void *stream) {
+    return guarded([&] {
+        tdz::Multigrid *mg = learned_mg(s);
+        TDZ_CHECK(lr > 0.f && std::isfinite(lr), TDZ_ERR_ARG, "learning rate must be positive");
+        const float l = mg->train_coarse(pairs, epochs, lr, seed, static_cast<cudaStream_t>(stream));
+        if (loss) *loss = l;
+    });
+}
+
+tdz_status tdz_solver_coarse_gain(tdz_solver *s, int trials, unsigned long long seed, double *plain,
+                                  double *learned, void *stream) {
+    return guarded([&] {
+        tdz::Multigrid *mg = learned_mg(s);
+        TDZ_CHECK(trials >= 1, TDZ_ERR_ARG, "trials must be positive");
+        const auto g = mg->coarse_gain(trials, seed, static_cast<cudaStream_t>(stream));
+        if (plain) *plain = g.first;
+        if (learned) *learned = g.second;
     });
 }
 

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "blas.h"
+#include "cnn.h"
 #include "krylov.h"
 #include "linesolve.h"
 #include "oper.h"
@@ -49,6 +50,21 @@ struct MGOptions {
     int coarse_its = 12;     // Chebyshev degree of the coarsest solve
     double ratio = 60.0;     // smoothing range [mu_hi / ratio, mu_hi]
     int precision = TDZ_FP32;
+    int learned = 0;         // 1: CNN correction of the coarsest solve (FP32 levels)
+};
+
+// Learned coarse correction: after the Chebyshev coarse solve x0 of A_c x = b_c,
+// x = x0 + s N(r / s) with r = b_c - A_c x0, s = ||r|| and N a 3D CNN on the
+// coarsest grid (2 channels: real, imaginary) trained on (r / s, A_c^-1 r / s)
+// pairs that the solver generates (tdz_solver_train_coarse). Until trained,
+// or with FP64 levels, the plain V-cycle runs.
+struct LearnedCoarse {
+    CNN net;
+    bool on = false, trained = false;
+    int width = 32, layers = 4, batch = 8;
+    DevBuf in, out, scale;       // planar [2][n] FP32 (batch 1), device ||r||
+    DevBuf pin, ptgt;            // training pairs [pairs][2][n]
+    int npairs = 0;
 };
 
 struct Multigrid : Precond {
@@ -59,13 +75,27 @@ struct Multigrid : Precond {
     DevBuf in32;                          // FP32 copy of the FP64 input
     long long cycles = 0;
     blas::Reducer red;
+    LearnedCoarse lrn;
 
     void setup(Operator *fine_, const MGOptions &o, cudaStream_t st);
     void estimate_bounds(cudaStream_t st);
     void vcycle(int l, cudaStream_t st);  // lv[l].b -> lv[l].x
+    // learned coarse correction (learned.cu)
+    void learned_setup();
+    void coarse_correct(MGLevel &m, cudaStream_t st);
+    // generate `pairs` pairs at the coarsest level for the current stage and
+    // train for `epochs` passes; returns the mean relative loss of the last epoch
+    float train_coarse(int pairs, int epochs, float lr, uint64_t seed, cudaStream_t st);
+    // relative error ||e - c|| / ||e|| of the corrected coarse solve c against
+    // e = A_c^-1 b on `trials` fresh random right-hand sides, without (first)
+    // and with (second) the network
+    std::pair<double, double> coarse_gain(int trials, uint64_t seed, cudaStream_t st);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;
     void refresh() override;
 };
+
+// Chebyshev iteration on the level's A x = b (mg_setup.cpp)
+void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, double w, int steps, bool x_zero, cudaStream_t st);
 
 // 1D helpers (mg_setup.cpp)
 std::vector<double> coarsen_knots(const std::vector<double> &U, bool *dropped);

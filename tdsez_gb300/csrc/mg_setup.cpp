@@ -218,6 +218,7 @@ void Multigrid::setup(Operator *fine_, const MGOptions &o, cudaStream_t st) {
     }
     red.init();
     estimate_bounds(st);
+    if (opt.learned) learned_setup();
 }
 
 namespace {
@@ -280,8 +281,6 @@ void Multigrid::estimate_bounds(cudaStream_t st) {
 
 void Multigrid::refresh() {}
 
-namespace {
-
 // Chebyshev iteration on A x = b with M^-1. The eigenvalues of M^-1 A are
 // alpha + g mu with mu = mu_r - i mu_i, mu_r in [mu_a, mu_b] (Hermitian part)
 // and mu_i in [0, w] (CAP). The iteration uses the ellipse that encloses this
@@ -334,13 +333,13 @@ void chebyshev(MGLevel &m, int prec, double mu_a, double mu_b, double w, int ste
     }
 }
 
-}  // namespace
 
 void Multigrid::vcycle(int l, cudaStream_t st) {
     MGLevel &m = lv[l];
     const int last = (int)lv.size() - 1;
     if (l == last) {
         chebyshev(m, prec, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);
+        if (lrn.on && lrn.trained) coarse_correct(m, st);
         return;
     }
     const double lo = m.mu_hi / opt.ratio;

