@@ -77,14 +77,15 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     static_assert(RY * (16 + 2 * P) <= kLoadsPerThread3 * 16 * TY, "tile larger than the prefetch registers");
     const int txw = blockDim.x;               // tile width of this launch
     const int NT = txw * TY, RXw = txw + 2 * P;
-    __shared__ C sIn[RY][RX];
-    __shared__ C sU[2][NU][RY][TX];
     __shared__ T sYm[BW][TY];
     __shared__ T sYs[HC ? BW : 1][TY];
     __shared__ C sYt[HB ? BW : 1][TY];
     extern __shared__ unsigned char dyn_raw[];
+    // dynamic: the halo tile, the double-buffered x-stage results, then the
     // precomputed outer-band rows of the chunk: [plane][o] (A, C complex; M real)
-    C *sZA = reinterpret_cast<C *>(dyn_raw);
+    C (*sIn)[RX] = reinterpret_cast<C (*)[RX]>(dyn_raw);
+    C (*sU)[NU][RY][TX] = reinterpret_cast<C (*)[NU][RY][TX]>(dyn_raw + sizeof(C) * RY * RX);
+    C *sZA = reinterpret_cast<C *>(dyn_raw + sizeof(C) * (RY * RX + 2 * NU * RY * TX));
     C *sZC = sZA + (size_t)prm.zchunk_planes * BW;
     T *sZM = reinterpret_cast<T *>(sZC + (HC ? (size_t)prm.zchunk_planes * BW : 0));
 
@@ -325,6 +326,12 @@ __global__ void k_apply1d(const ApplyParams<T> prm) {
 
 // ---------------------------------------------------------------- launch helpers
 constexpr int kTX3 = 32, kTY3 = 8, kTX2 = 128;
+// tile height: 8 rows for FP32; 16 for FP64 and double-float, which recompute
+// the 2p halo rows of the x stage (ratio (16 + 2p) / 16 instead of (8 + 2p) / 8),
+// except with all three streams, whose registers need the smaller CTA
+template <class T, bool HB, bool HC> struct TileY {
+    static constexpr int v = std::is_same<T, float>::value || (HB && HC) ? 8 : 16;
+};
 
 // z chunk per CTA: about `target` CTAs in total, chunks no shorter than 4p
 // planes (the 2p halo planes of a chunk are re-read)
@@ -363,22 +370,25 @@ template <class T, int P, bool HB, bool HC>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     using C = typename CT<T>::type;
     ApplyParams<T> prm = prm0;
-    auto kern = k_apply3d<T, P, HB, HC, kTX3, kTY3>;
+    constexpr int TY = TileY<T, HB, HC>::v, NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
+    auto kern = k_apply3d<T, P, HB, HC, kTX3, TY>;
     // FP32 (HBM-leaning): full warps along x, about 8 CTAs per SM. FP64 and
     // double-float (FP64/FP32-pipe bound): the tile width with the least x
     // padding and the z chunking with the fewest waves x (chunk + halo).
     const bool fp32 = std::is_same<T, float>::value;
     const int txw = fp32 ? kTX3 : pick_tile_x(prm.n0);
-    const int tiles = ((prm.n0 + txw - 1) / txw) * ((prm.n1 + kTY3 - 1) / kTY3);
+    const int tiles = ((prm.n0 + txw - 1) / txw) * ((prm.n1 + TY - 1) / TY);
+    const size_t tile_smem = sizeof(C) * ((size_t)(TY + 2 * P) * (kTX3 + 2 * P) + 2 * NU * (TY + 2 * P) * kTX3);
     if (fp32) {
         prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P), 96);
     } else {
         static int slots = 0;   // resident CTAs on the GPU at the largest dynamic smem (96-plane chunks)
         if (!slots) {
-            const size_t smax = (size_t)(96 + 2 * P) * (2 * P + 1) * (sizeof(C) * (HC ? 2 : 1) + (HB ? sizeof(T) : 0));
+            const size_t smax =
+                tile_smem + (size_t)(96 + 2 * P) * (2 * P + 1) * (sizeof(C) * (HC ? 2 : 1) + (HB ? sizeof(T) : 0));
             TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
             int per_sm = 0, dev = 0, nsm = 0;
-            TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, txw * kTY3, smax));
+            TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, txw * TY, smax));
             TDZ_CUDA(cudaGetDevice(&dev));
             TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
             slots = std::max(1, per_sm) * nsm;
@@ -387,7 +397,7 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     }
     prm.zchunk_planes = prm.zchunk + 2 * P;
     const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
-    const size_t smem = rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
+    const size_t smem = tile_smem + rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
     // static + dynamic shared memory above 48 KB needs the opt-in (set once per size increase)
     static size_t opted = 0;
     if (smem > opted) {
@@ -395,7 +405,7 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
         opted = smem;
     }
     dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
-    kern<<<grid, dim3(txw, kTY3), smem, st>>>(prm);
+    kern<<<grid, dim3(txw, TY), smem, st>>>(prm);
 }
 
 template <class T, int P, bool HB, bool HC>

@@ -202,6 +202,52 @@ __global__ void k_add_cast_df(double2 *y, cdff a, const float2 *x, size_t n) {
 
 inline cdff cdf_host(cd a) { return mk_df(dff_from(a.real()), dff_from(a.imag())); }
 
+// Fused Gram-Schmidt pass on an Arnoldi vector: w += sum_i a_i V_i (the
+// result kept to 48 bits, the precision of the basis), then in the same pass
+// either the dots conj(V_i) w (NORM = false, partial slots 0..K-1) or |w|^2
+// (NORM = true, slot 0): one read of V and w instead of two.
+template <int K, bool NORM>
+__global__ void __launch_bounds__(kThreads) k_gs_df(double2 *w, PtrPack V, CoefDF a, size_t n, double2 *partial) {
+    constexpr int R = NORM ? 1 : K;
+    cdff acc[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) acc[i] = czero<cdff>();
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        cdff v[K];
+        cdff x = ld_df(w[e]);
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            v[i] = ld_df(static_cast<const double2 *>(V.p[i])[e]);
+            cfma(x, mk_df(a.re[i], a.im[i]), v[i]);
+        }
+        x = cnorm(x);
+        w[e] = st_df(x);
+        if constexpr (NORM) {
+            cfma_conj(acc[0], x, x);
+        } else {
+#pragma unroll
+            for (int i = 0; i < K; ++i) cfma_conj(acc[i], v[i], x);
+        }
+    }
+    __shared__ double2 red[kThreads / 32][R];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        double re = dff_to_double(acc[i].x), im = dff_to_double(acc[i].y);
+        for (int off = 16; off > 0; off >>= 1) {
+            re += __shfl_down_sync(0xffffffffu, re, off);
+            im += __shfl_down_sync(0xffffffffu, im, off);
+        }
+        if (lane == 0) red[warp][i] = make_double2(re, im);
+    }
+    __syncthreads();
+    if (threadIdx.x < R) {
+        double re = 0.0, im = 0.0;
+        for (int w2 = 0; w2 < kThreads / 32; ++w2) { re += red[w2][threadIdx.x].x; im += red[w2][threadIdx.x].y; }
+        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_double2(re, im);
+    }
+}
+
 // per-block partial sums of conj(V_i) w, i < k; partial layout [i][block]
 template <class T, int K>
 __global__ void __launch_bounds__(kThreads) k_mdot(PtrPack V, const typename CT<T>::type *w, size_t n,
@@ -439,6 +485,46 @@ void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec
         else maxpy_dispatch<float>(kk, w, pp, cp, n, st);
         TDZ_CUDA(cudaGetLastError());
     count_launch();
+    }
+}
+
+void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, size_t n, cd *dots, double *norm,
+               cudaStream_t st) {
+    TDZ_CHECK(k >= 1 && k <= kMaxDot, TDZ_ERR_INTERNAL, "fused Gram-Schmidt width");
+    TDZ_CHECK((dots != nullptr) != (norm != nullptr), TDZ_ERR_INTERNAL, "dots or norm");
+    r.init();
+    PtrPack pp{};
+    CoefPack cp{};
+    for (int i = 0; i < k; ++i) {
+        pp.p[i] = V[i];
+        cp.re[i] = a[i].real();
+        cp.im[i] = a[i].imag();
+    }
+    const CoefDF cd_ = coef_df(cp, k);
+    double2 *wp = static_cast<double2 *>(w);
+    double2 *part = r.partial.as<double2>();
+    switch (k) {
+#define TDZ_CASE(K)                                                                                       \
+    case K:                                                                                               \
+        if (norm) k_gs_df<K, true><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);                  \
+        else k_gs_df<K, false><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);                      \
+        break;
+        TDZ_CASE(1) TDZ_CASE(2) TDZ_CASE(3) TDZ_CASE(4) TDZ_CASE(5) TDZ_CASE(6) TDZ_CASE(7) TDZ_CASE(8)
+        TDZ_CASE(9) TDZ_CASE(10) TDZ_CASE(11) TDZ_CASE(12) TDZ_CASE(13) TDZ_CASE(14) TDZ_CASE(15) TDZ_CASE(16)
+#undef TDZ_CASE
+    default: break;
+    }
+    const int nres = norm ? 1 : k;
+    k_finish<<<nres, kThreads, 0, st>>>(part, r.blocks, r.result.as<double2>());
+    TDZ_CUDA(cudaGetLastError());
+    count_launch(2);
+    TDZ_CUDA(cudaMemcpyAsync(r.host, r.result.ptr, sizeof(double2) * nres, cudaMemcpyDeviceToHost, st));
+    TDZ_CUDA(cudaStreamSynchronize(st));
+    if (norm) {
+        const double v = r.host[0].x;
+        *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
+    } else {
+        for (int i = 0; i < k; ++i) dots[i] = cd(r.host[i].x, r.host[i].y);
     }
 }
 

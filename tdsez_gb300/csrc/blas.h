@@ -49,6 +49,10 @@ constexpr int kRedBlocksPublic = 2 * 152;   // blocks of the reductions (partial
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st);
 // ||x||_2 (synchronises)
 double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st);
+// FP64 Arnoldi vector, fused Gram-Schmidt pass (k <= 16): w += sum_i a_i V_i,
+// then either dots[i] = <V_i, w> or *norm = ||w|| from the same pass
+void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, size_t n, cd *dots, double *norm,
+               cudaStream_t st);
 
 }  // namespace blas
 

@@ -68,15 +68,23 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             double2 *wv = w.as<double2>();
             op->apply(TDZ_STAGE, aprec, zj, wv, st);
             ++applies;
-            // CGS with one re-orthogonalisation
+            // CGS with one re-orthogonalisation; up to 16 basis vectors the
+            // update and the next reduction share one pass over V and w
+            double hn = 0.0;
             blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h.data(), st);
             for (int i = 0; i <= j; ++i) h[i] = -h[i];
-            blas::maxpy(wv, j + 1, Vp.data(), h.data(), n, TDZ_FP64, st);
-            blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h2.data(), st);
-            for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
-            blas::maxpy(wv, j + 1, Vp.data(), h2.data(), n, TDZ_FP64, st);
+            if (j + 1 <= 16) {
+                blas::gs_update(red, wv, j + 1, Vp.data(), h.data(), n, h2.data(), nullptr, st);
+                for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
+                blas::gs_update(red, wv, j + 1, Vp.data(), h2.data(), n, nullptr, &hn, st);
+            } else {
+                blas::maxpy(wv, j + 1, Vp.data(), h.data(), n, TDZ_FP64, st);
+                blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h2.data(), st);
+                for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
+                blas::maxpy(wv, j + 1, Vp.data(), h2.data(), n, TDZ_FP64, st);
+                hn = blas::nrm2(red, wv, n, TDZ_FP64, st);
+            }
             for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = -(h[i] + h2[i]);
-            const double hn = blas::nrm2(red, wv, n, TDZ_FP64, st);
             if (!std::isfinite(hn)) { s.reason = -9; done = true; break; }
             H[(size_t)(j + 1) * m + j] = hn;
             // apply previous rotations to column j
