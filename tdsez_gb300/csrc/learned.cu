@@ -3,14 +3,14 @@
 // The coarsest level of the V-cycle is solved by a Chebyshev polynomial
 // (the reference factorises it with MUMPS, src/multigrid.cpp:315-324, which
 // has no GPU counterpart here). The network corrects that solve:
-//   x = x0 + s N(r / s),  r = b_c - A_c x0,  s = ||r||,
+//   x = x0 + c rms(r) N(r / rms(r)),  r = b_c - A_c x0,  c = mean ||e|| / ||r||,
 // N a 3D CNN (cnn.cu: 3x3x3 convolutions, BF16 weights, FP32 accumulation)
 // on the coarsest grid with the real and imaginary parts as channels. The
-// training pairs (r / s, e / s), e = A_c^-1 r, come from the solver itself:
-// random coarse right-hand sides, the production Chebyshev solve, and a
-// 10x longer Chebyshev solve for e. Everything stays on the device in the
-// V-cycle (the scale s is a device scalar), so the corrected cycle needs no
-// host synchronisation.
+// training pairs (r / rms(r), e / (c rms(r))), e = A_c^-1 r, come from the
+// solver itself: random coarse right-hand sides, the production Chebyshev
+// solve, and a 10x longer Chebyshev solve for e. Everything stays on the
+// device in the V-cycle (rms(r) is a device scalar), so the corrected cycle
+// needs no host synchronisation.
 #include <cmath>
 #include <random>
 
@@ -35,31 +35,32 @@ __global__ void k_norm_one(const float2 *r, int n, float *s) {
     if (threadIdx.x == 0) *s = sqrtf(red[0]);
 }
 
-// planar [2][n] = r / s (0 when s = 0)
+// planar [2][n] = r / rms(r) (unit-RMS network input; 0 when r = 0)
 __global__ void k_pack(const float2 *r, int n, const float *s, float *out) {
-    const float inv = *s > 0.f ? 1.f / *s : 0.f;
+    const float inv = *s > 0.f ? sqrtf(2.f * n) / *s : 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         out[i] = r[i].x * inv;
         out[n + i] = r[i].y * inv;
     }
 }
 
-// x += s (out[0] + i out[1])
-__global__ void k_unpack_add(float2 *x, int n, const float *s, const float *out) {
-    const float sc = *s;
+// x += rms(r) c (out[0] + i out[1])
+__global__ void k_unpack_add(float2 *x, int n, const float *s, float c, const float *out) {
+    const float sc = *s * c / sqrtf(2.f * n);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x[i].x += sc * out[i];
         x[i].y += sc * out[n + i];
     }
 }
 
-// training pair: in = r / s, target = e / s
-__global__ void k_pack_pair(const float2 *r, const float2 *e, int n, float inv, float *in, float *tgt) {
+// training pair: in = r / rms(r), target = e / (rms(r) c)
+__global__ void k_pack_pair(const float2 *r, const float2 *e, int n, float in_scale, float tgt_scale, float *in,
+                            float *tgt) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        in[i] = r[i].x * inv;
-        in[n + i] = r[i].y * inv;
-        tgt[i] = e[i].x * inv;
-        tgt[n + i] = e[i].y * inv;
+        in[i] = r[i].x * in_scale;
+        in[n + i] = r[i].y * in_scale;
+        tgt[i] = e[i].x * tgt_scale;
+        tgt[n + i] = e[i].y * tgt_scale;
     }
 }
 
@@ -105,7 +106,8 @@ void Multigrid::coarse_correct(MGLevel &m, cudaStream_t st) {
     k_norm_one<<<1, 256, 0, st>>>(m.r.as<float2>(), n, lrn.scale.as<float>());
     k_pack<<<blocks_for(n), 256, 0, st>>>(m.r.as<float2>(), n, lrn.scale.as<float>(), lrn.in.as<float>());
     lrn.net.forward(lrn.in.as<float>(), lrn.out.as<float>(), 1, st, false);
-    k_unpack_add<<<blocks_for(n), 256, 0, st>>>(m.x.as<float2>(), n, lrn.scale.as<float>(), lrn.out.as<float>());
+    k_unpack_add<<<blocks_for(n), 256, 0, st>>>(m.x.as<float2>(), n, lrn.scale.as<float>(), lrn.cscale,
+                                                lrn.out.as<float>());
     TDZ_CUDA(cudaGetLastError());
     count_launch(3);
 }
@@ -124,6 +126,8 @@ float Multigrid::train_coarse(int pairs, int epochs, float lr, uint64_t seed, cu
     lrn.npairs = pairs;
     std::mt19937_64 rng(seed);
     DevBuf x0(m.ndof * sizeof(float2)), r(m.ndof * sizeof(float2));
+    const double root = std::sqrt(2.0 * n);
+    double ratio_sum = 0.0;
     for (int k = 0; k < pairs; ++k) {
         random_rhs(m.b, m.ndof, rng, st);
         chebyshev(m, TDZ_FP32, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);   // production solve
@@ -132,10 +136,15 @@ float Multigrid::train_coarse(int pairs, int epochs, float lr, uint64_t seed, cu
         blas::axpbypcz(r.ptr, 1.0, m.b.ptr, 0.0, m.t1.ptr, -1.0, m.ndof, TDZ_FP32, st);   // r = b - A x0
         blas::copy(r.ptr, m.b.ptr, m.ndof, TDZ_FP32, st);
         chebyshev(m, TDZ_FP32, m.mu_lo, m.mu_hi, m.w_max, 10 * opt.coarse_its, true, st);   // e = A^-1 r
-        const double s = norm_host(r, m.ndof, st);
-        const float inv = s > 0.0 ? (float)(1.0 / s) : 0.f;
-        k_pack_pair<<<blocks_for(n), 256, 0, st>>>(r.as<float2>(), m.x.as<float2>(), n, inv,
-                                                  lrn.pin.as<float>() + (size_t)k * per,
+        const double s = norm_host(r, m.ndof, st), se = norm_host(m.x, m.ndof, st);
+        // global target scale c = mean ||e|| / ||r|| over the first pairs, so targets are O(1) too
+        if (k < 32) {
+            ratio_sum += s > 0.0 ? se / s : 0.0;
+            lrn.cscale = (float)std::max(ratio_sum / (k + 1), 1e-30);
+        }
+        const float in_scale = s > 0.0 ? (float)(root / s) : 0.f;
+        k_pack_pair<<<blocks_for(n), 256, 0, st>>>(r.as<float2>(), m.x.as<float2>(), n, in_scale,
+                                                  in_scale / lrn.cscale, lrn.pin.as<float>() + (size_t)k * per,
                                                   lrn.ptgt.as<float>() + (size_t)k * per);
         TDZ_CUDA(cudaGetLastError());
     }

@@ -54,9 +54,12 @@ struct MGOptions {
 };
 
 // Learned coarse correction: after the Chebyshev coarse solve x0 of A_c x = b_c,
-// x = x0 + s N(r / s) with r = b_c - A_c x0, s = ||r|| and N a 3D CNN on the
-// coarsest grid (2 channels: real, imaginary) trained on (r / s, A_c^-1 r / s)
-// pairs that the solver generates (tdz_solver_train_coarse). Until trained,
+// x = x0 + c rms(r) N(r / rms(r)) with r = b_c - A_c x0, c = the training pairs'
+// mean ||e|| / ||r||, and N a 3D CNN on the
+// coarsest grid (2 channels: real, imaginary) trained on (r / rms(r),
+// A_c^-1 r / (c rms(r))) pairs that the solver generates
+// (tdz_solver_train_coarse). Unit-RMS inputs and O(1) targets keep the
+// ReLU network away from the zero-output collapse. Until trained,
 // or with FP64 levels, the plain V-cycle runs.
 struct LearnedCoarse {
     CNN net;
@@ -65,6 +68,7 @@ struct LearnedCoarse {
     DevBuf in, out, scale;       // planar [2][n] FP32 (batch 1), device ||r||
     DevBuf pin, ptgt;            // training pairs [pairs][2][n]
     int npairs = 0;
+    float cscale = 1.f;          // mean ||e|| / ||r|| of the training pairs (output scale)
 };
 
 struct Multigrid : Precond {

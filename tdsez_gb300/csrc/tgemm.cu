@@ -1,8 +1,9 @@
 // tcgen05 transform kernel (see tgemm.h).
 //
-// Persistent CTAs (one per SM, 160 threads) walk 128 x Np output tiles (64
-// complex rows, real and imaginary part rows interleaved); the accumulator
-// lives in tensor memory (TMEM, Np <= 256 FP32 columns). K runs in chunks of
+// Persistent CTAs (one per SM, 160 threads) walk 256 x Np output tiles (two
+// 128-row sub-tiles; 128 x Np when Np > 192), 64 complex rows per sub-tile with
+// real and imaginary part rows interleaved; the accumulators live in tensor
+// memory (TMEM, columns 0 and 256). K runs in chunks of
 // 32 (one 128-byte swizzled row per operand row) through an NS-stage ring
 // (NS = 3, or 2 for Np > 192) that warp 4 fills with TMA
 // (cp.async.bulk.tensor, 128-byte swizzle) up to NS chunks ahead, across tile
@@ -146,36 +147,41 @@ __device__ __forceinline__ void bar_sync(int id, int count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-template <int NP> struct TGShape {
+// MS = 128-row sub-tiles per tile (1 or 2): with 2, each B chunk loaded by TMA
+// serves 256 rows (two accumulators in TMEM at columns 0 and 256)
+template <int NP, int MS> struct TGShape {
     static constexpr int B_BYTES = NP * KC * 4;
-    static constexpr int STAGE = A_BYTES + 2 * B_BYTES;          // A (FP32 -> TF32 hi in place), B hi, B lo
-    static constexpr int NS = 3 * STAGE + 2 * A_BYTES + 1100 <= 232448 ? 3 : 2;
-    static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 2 * A_BYTES + 2 * NS * 8 + 16;
+    static constexpr int A_T = MS * A_BYTES;
+    static constexpr int STAGE = A_T + 2 * B_BYTES;          // A (FP32 -> TF32 hi in place), B hi, B lo
+    static constexpr int NS = 3 * STAGE + 2 * A_T + 1100 <= 232448 ? 3 : 2;
+    static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 2 * A_T + 2 * NS * 8 + 16;
+    static constexpr bool fits = SMEM <= 232448;
 };
 
 // Persistent, warp-specialised: warps 0-3 split A, issue the MMAs (thread 0)
 // and run the epilogue; warp 4 (one lane) is the TMA producer, running up to
 // NS chunks ahead across tile boundaries, so loads overlap the epilogue.
-template <int NP>
+template <int NP, int MS>
 __global__ void __launch_bounds__(160, 1)
     k_transform(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap, const TGParams prm) {
-    using S = TGShape<NP>;
-    constexpr int NS = S::NS, STAGE = S::STAGE, B_BYTES = S::B_BYTES;
-    constexpr uint32_t TMEM_COLS = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;
+    using S = TGShape<NP, MS>;
+    constexpr int NS = S::NS, STAGE = S::STAGE, B_BYTES = S::B_BYTES, A_T = S::A_T, TMT = TM * MS;
+    constexpr uint32_t TMEM_COLS = MS == 2 ? 512 : NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;
     static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N tile");
+    static_assert(S::fits, "shared memory");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *alo_base = base + NS * STAGE;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(alo_base + 2 * A_BYTES);   // full[NS], done[NS]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(alo_base + 2 * A_T);   // full[NS], done[NS]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nch = prm.nchunks;
     const int my_tiles = prm.tiles > (int)blockIdx.x ? (prm.tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int G = my_tiles * nch;
     auto a_st = [&](int s) { return base + s * STAGE; };
-    auto bh_st = [&](int s) { return base + s * STAGE + A_BYTES; };
-    auto bl_st = [&](int s) { return base + s * STAGE + A_BYTES + B_BYTES; };
-    auto a_lo = [&](int g) { return alo_base + (g & 1) * A_BYTES; };
+    auto bh_st = [&](int s) { return base + s * STAGE + A_T; };
+    auto bl_st = [&](int s) { return base + s * STAGE + A_T + B_BYTES; };
+    auto a_lo = [&](int g) { return alo_base + (g & 1) * A_T; };
     const uint32_t full0 = smem_u32(&bars[0]), done0 = smem_u32(&bars[NS]);
 
     if (tid == 0) {
@@ -199,13 +205,13 @@ __global__ void __launch_bounds__(160, 1)
     if (warp == 4) {
         // ---- producer
         if (lane == 0) {
-            constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
+            constexpr uint32_t TX = A_T + 2 * B_BYTES;
             for (int g = 0; g < G; ++g) {
                 const int s = g % NS;
                 if (g >= NS && !mbar_wait(done0 + 8 * s, ((g - NS) / NS) & 1)) break;
                 const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x, c = g % nch;
                 mbar_expect_tx(full0 + 8 * s, TX);
-                tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TM, full0 + 8 * s);
+                tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TMT, full0 + 8 * s);
                 tma_load_2d(smem_u32(bh_st(s)), &bmap, c * KC, 0, full0 + 8 * s);
                 tma_load_2d(smem_u32(bl_st(s)), &bmap, c * KC, NP, full0 + 8 * s);
             }
@@ -222,7 +228,7 @@ __global__ void __launch_bounds__(160, 1)
             float4 *ah = reinterpret_cast<float4 *>(a_st(s));
             float4 *al = reinterpret_cast<float4 *>(a_lo(g));
 #pragma unroll
-            for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
+            for (int q = 0; q < A_T / 16 / 128; ++q) {
                 const int e = tid + q * 128;
                 const float4 v = ah[e];
                 const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
@@ -239,11 +245,15 @@ __global__ void __launch_bounds__(160, 1)
 #pragma unroll
                 for (int j = 0; j < KC / 8; ++j) {
                     const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the swizzled row
-                    const uint64_t dah = smem_desc(ah_a + off), dal = smem_desc(al_a + off);
                     const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
-                    mma_tf32(tmem, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
-                    mma_tf32(tmem, dah, dbl, idesc, 1u);
-                    mma_tf32(tmem, dal, dbh, idesc, 1u);
+#pragma unroll
+                    for (int t = 0; t < MS; ++t) {   // sub-tile t: A rows 128 t.., accumulator columns 256 t..
+                        const uint64_t dah = smem_desc(ah_a + t * A_BYTES + off), dal = smem_desc(al_a + t * A_BYTES + off);
+                        const uint32_t d = tmem + (uint32_t)(t * 256);
+                        mma_tf32(d, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                        mma_tf32(d, dah, dbl, idesc, 1u);
+                        mma_tf32(d, dal, dbh, idesc, 1u);
+                    }
                 }
                 mma_commit(done0 + 8 * s);
             }
@@ -253,29 +263,32 @@ __global__ void __launch_bounds__(160, 1)
                 if (!bar_and(1, 128, okd)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x;
-                const int row = tile * TM + warp * 32 + lane;
-                const bool row_ok = row < prm.rows;
-                const int cr = row >> 1, part = row & 1;
-                const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
-                float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
                 const size_t nstride = (size_t)2 * prm.ldo;
 #pragma unroll 1
-                for (int c0 = 0; c0 < NP; c0 += 16) {
-                    uint32_t v[16];
-                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15}, [%16];"
-                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                          "=r"(v[14]), "=r"(v[15])
-                        : "r"(taddr));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (row_ok) {
+                for (int t = 0; t < MS; ++t) {
+                    const int row = tile * TMT + t * TM + warp * 32 + lane;
+                    const bool row_ok = row < prm.rows;
+                    const int cr = row >> 1, part = row & 1;
+                    const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
+                    float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
+#pragma unroll 1
+                    for (int c0 = 0; c0 < NP; c0 += 16) {
+                        uint32_t v[16];
+                        const uint32_t taddr = tmem + (uint32_t)(t * 256) + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                            "%12, %13, %14, %15}, [%16];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                              "=r"(v[14]), "=r"(v[15])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        if (row_ok) {
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const int n = c0 + j;
-                            if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+                            for (int j = 0; j < 16; ++j) {
+                                const int n = c0 + j;
+                                if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+                            }
                         }
                     }
                 }
@@ -340,15 +353,23 @@ int sm_count() {
     return n;
 }
 
-template <int NP> void launch(const TransformMat &T, const CUtensorMap &amap, const TGParams &prm, cudaStream_t st) {
-    const size_t smem = TGShape<NP>::SMEM;
+// 256-row tiles where two sub-tiles' stages fit in shared memory (Np <= 192), else 128
+template <int NP> constexpr int sub_tiles() { return TGShape<NP, 2>::fits ? 2 : 1; }
+
+template <int NP>
+void launch(const TransformMat &T, const float *in, int ldi, TGParams prm, cudaStream_t st) {
+    constexpr int MS = sub_tiles<NP>();
+    const size_t smem = TGShape<NP, MS>::SMEM;
     static bool attr = false;   // set once per process (same device attribute for every device)
     if (!attr) {
-        TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
+    CUtensorMap amap;
+    make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)(TM * MS));
+    prm.tiles = (prm.rows + TM * MS - 1) / (TM * MS);
     const int grid = std::min(prm.tiles, sm_count());
-    k_transform<NP><<<grid, 160, smem, st>>>(amap, T.map, prm);
+    k_transform<NP, MS><<<grid, 160, smem, st>>>(amap, T.map, prm);
 }
 
 }  // namespace
@@ -389,8 +410,6 @@ void transform(const TransformMat &T, const float *in, int planes, int R, int ld
     TDZ_CHECK(ldi >= T.K && ldo >= R, TDZ_ERR_ARG, "transform pitches too small");
     const long long rows = 2LL * planes * R;
     TDZ_CHECK(rows < (1LL << 31), TDZ_ERR_ARG, "transform too large");
-    CUtensorMap amap;
-    make_map(&amap, in, (uint64_t)T.K, (uint64_t)rows, (uint64_t)ldi, TM);
     TGParams prm{};
     prm.out = out;
     prm.rows = (int)rows;
@@ -398,24 +417,23 @@ void transform(const TransformMat &T, const float *in, int planes, int R, int ld
     prm.N = T.N;
     prm.ldo = ldo;
     prm.nchunks = T.Kp / KC;
-    prm.tiles = (int)((rows + TM - 1) / TM);
     switch (T.Np) {
-    case 16: launch<16>(T, amap, prm, st); break;
-    case 32: launch<32>(T, amap, prm, st); break;
-    case 48: launch<48>(T, amap, prm, st); break;
-    case 64: launch<64>(T, amap, prm, st); break;
-    case 80: launch<80>(T, amap, prm, st); break;
-    case 96: launch<96>(T, amap, prm, st); break;
-    case 112: launch<112>(T, amap, prm, st); break;
-    case 128: launch<128>(T, amap, prm, st); break;
-    case 144: launch<144>(T, amap, prm, st); break;
-    case 160: launch<160>(T, amap, prm, st); break;
-    case 176: launch<176>(T, amap, prm, st); break;
-    case 192: launch<192>(T, amap, prm, st); break;
-    case 208: launch<208>(T, amap, prm, st); break;
-    case 224: launch<224>(T, amap, prm, st); break;
-    case 240: launch<240>(T, amap, prm, st); break;
-    case 256: launch<256>(T, amap, prm, st); break;
+    case 16: launch<16>(T, in, ldi, prm, st); break;
+    case 32: launch<32>(T, in, ldi, prm, st); break;
+    case 48: launch<48>(T, in, ldi, prm, st); break;
+    case 64: launch<64>(T, in, ldi, prm, st); break;
+    case 80: launch<80>(T, in, ldi, prm, st); break;
+    case 96: launch<96>(T, in, ldi, prm, st); break;
+    case 112: launch<112>(T, in, ldi, prm, st); break;
+    case 128: launch<128>(T, in, ldi, prm, st); break;
+    case 144: launch<144>(T, in, ldi, prm, st); break;
+    case 160: launch<160>(T, in, ldi, prm, st); break;
+    case 176: launch<176>(T, in, ldi, prm, st); break;
+    case 192: launch<192>(T, in, ldi, prm, st); break;
+    case 208: launch<208>(T, in, ldi, prm, st); break;
+    case 224: launch<224>(T, in, ldi, prm, st); break;
+    case 240: launch<240>(T, in, ldi, prm, st); break;
+    case 256: launch<256>(T, in, ldi, prm, st); break;
     default: throw Error(TDZ_ERR_INTERNAL, "bad transform tile width");
     }
     TDZ_CUDA(cudaGetLastError());

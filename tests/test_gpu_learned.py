@@ -27,7 +27,7 @@ def test_learned_coarse_correction(cuda):
     assert reason > 0
 
     s = Solver(op, pc="mg", precision="fp32", rtol=1e-10, maxit=200, mg_learned=True)
-    loss = s.train_coarse(pairs=512, epochs=30, lr=1e-3, seed=3)
+    loss = s.train_coarse(pairs=512, epochs=60, lr=1e-3, seed=3)
     assert np.isfinite(loss) and loss < 1.0
     e_plain, e_learned = s.coarse_gain(trials=16, seed=99)
     print(f"coarse solve error: Chebyshev {e_plain:.3e}, with the network {e_learned:.3e}; training loss {loss:.3e}")
