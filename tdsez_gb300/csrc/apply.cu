@@ -24,6 +24,17 @@ CombP<T> eval_comb(const Comb &c, const std::array<cd, 5> &sg) {
     return out;
 }
 
+// 1: every coefficient of the combination is real, 2: every one is imaginary, else 0
+inline int comb_kind(const Comb &c, const std::array<cd, 5> &sg) {
+    bool re = true, im = true;
+    for (int i = 0; i < c.n; ++i) {
+        const cd v = c.factor[i] * sg[c.scalar[i]];
+        if (v.imag() != 0.0) re = false;
+        if (v.real() != 0.0) im = false;
+    }
+    return re ? 1 : im ? 2 : 0;
+}
+
 template <class T> const DevBuf &bands_of(const Operator &op, int d) {
     if (std::is_same<T, double>::value) return op.dev64[d];
     if (std::is_same<T, dff>::value) return op.devdf[d];
@@ -47,6 +58,8 @@ ApplyParams<T> make_params(const Operator &op, const Plan &pl, const void *x, vo
     prm.yT = eval_comb<T>(pl.yT, sg);
     prm.zA = eval_comb<T>(pl.zA, sg);
     prm.zC = eval_comb<T>(pl.zC, sg);
+    prm.za_kind = comb_kind(pl.zA, sg);
+    prm.zc_kind = comb_kind(pl.zC, sg);
     prm.p = s.ax[0].p;
     prm.walls = 0;
     if (pl.walls) {

@@ -44,6 +44,7 @@ template <class T> struct ApplyParams {
     int p;                      // degree (1D kernel)
     T wall_re[2], wall_im[2];   // 1D walls: diagonal values, wall = 0 / n-1
     int walls;
+    int za_kind, zc_kind;       // outer combinations: 0 complex, 1 real, 2 imaginary (fewer products)
 };
 
 // entry o of row i of a combination of base bands
@@ -128,20 +129,29 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
         if constexpr (HB) sZM[i] = in ? prm.b2[((size_t)kM * n2 + zin) * BW + o] : T(0);
     }
 
-    // prefetch registers: element e = tid + q NT of the (RY x RX) tile
+    // prefetch registers: element e = tid + q NT of the (RY x RX) tile. The
+    // element's place in the plane and in sIn is the same for every plane, so
+    // it is resolved once here (off: in-plane offset, -1 outside the grid or
+    // the tile; so: slot in sIn, -1 outside the tile).
     C pre[kLoadsPerThread3];
+    int off[kLoadsPerThread3], so[kLoadsPerThread3];
+#pragma unroll
+    for (int q = 0; q < kLoadsPerThread3; ++q) {
+        const int e = tid + q * NT;
+        off[q] = -1;
+        so[q] = -1;
+        if (e < RY * RXw) {
+            const int r = e / RXw, c = e % RXw;
+            so[q] = r * RX + c;
+            const int yy = y0 - P + r, xx = x0 - P + c;
+            if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) off[q] = yy * n0 + xx;
+        }
+    }
+    const size_t plane = (size_t)n1 * n0;
     auto load_plane = [&](int zin) {
 #pragma unroll
-        for (int q = 0; q < kLoadsPerThread3; ++q) {
-            const int e = tid + q * NT;
-            C v = czero<C>();
-            if (e < RY * RXw) {
-                const int r = e / RXw, c = e % RXw;
-                const int yy = y0 - P + r, xx = x0 - P + c;
-                if (yy >= 0 && yy < n1 && xx >= 0 && xx < n0) v = load_c<C>(X[((size_t)zin * n1 + yy) * n0 + xx]);
-            }
-            pre[q] = v;
-        }
+        for (int q = 0; q < kLoadsPerThread3; ++q)
+            pre[q] = off[q] >= 0 ? load_c<C>(X[(size_t)zin * plane + off[q]]) : czero<C>();
     };
     const int zfirst = max(zs, 0);
     load_plane(zfirst);
@@ -159,10 +169,8 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
             if (zin >= 0 && zin < n2) {
                 const int buf = it & 1;
 #pragma unroll
-                for (int q = 0; q < kLoadsPerThread3; ++q) {
-                    const int e = tid + q * NT;
-                    if (e < RY * RXw) sIn[e / RXw][e % RXw] = pre[q];
-                }
+                for (int q = 0; q < kLoadsPerThread3; ++q)
+                    if (so[q] >= 0) (&sIn[0][0])[so[q]] = pre[q];
                 __syncthreads();
                 if (zin + 1 < n2 && zin + 1 < z1 + P) load_plane(zin + 1);
                 // x stage
@@ -204,9 +212,9 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
 #pragma unroll
                 for (int o = 0; o < BW; ++o) {
                     C &a = acc[(ph - P + o + 2 * BW) % BW];
-                    cfma(a, zA[o], wA);
+                    kfma(a, zA[o], wA, prm.za_kind);
                     if constexpr (HB) rfma(a, sZM[(size_t)it * BW + o], wB);
-                    if constexpr (HC) cfma(a, sZC[(size_t)it * BW + o], wC);
+                    if constexpr (HC) kfma(a, sZC[(size_t)it * BW + o], wC, prm.zc_kind);
                 }
             }
             if (it >= 2 * P) {
@@ -282,9 +290,9 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
 #pragma unroll
                 for (int o = 0; o < BW; ++o) {
                     C &a = acc[(ph - P + o + 2 * BW) % BW];
-                    cfma(a, sZA[o], uM);
+                    kfma(a, sZA[o], uM, prm.za_kind);
                     if constexpr (HB) rfma(a, sZM[o], uT);
-                    if constexpr (HC) cfma(a, sZC[o], uS);
+                    if constexpr (HC) kfma(a, sZC[o], uS, prm.zc_kind);
                 }
             }
             if (it >= 2 * P) {

@@ -122,6 +122,17 @@ template <class C> __device__ __forceinline__ void cfma(C &acc, C a, C v) {
     acc.y = tfma(a.x, v.y, acc.y);
     acc.y = tfma(a.y, v.x, acc.y);
 }
+// acc += i b v (b real: the imaginary part of a purely imaginary coefficient)
+template <class T, class C> __device__ __forceinline__ void ifma(C &acc, T b, C v) {
+    acc.x = tfma(-b, v.y, acc.x);
+    acc.y = tfma(b, v.x, acc.y);
+}
+// acc += a v with a of a known kind: 0 complex, 1 real, 2 imaginary
+template <class C> __device__ __forceinline__ void kfma(C &acc, C a, C v, int kind) {
+    if (kind == 1) rfma(acc, a.x, v);
+    else if (kind == 2) ifma(acc, a.y, v);
+    else cfma(acc, a, v);
+}
 // acc += conj(a) v
 template <class C> __device__ __forceinline__ void cfma_conj(C &acc, C a, C v) {
     acc.x = tfma(a.x, v.x, acc.x);

@@ -1,8 +1,18 @@
-"""Learned coarse correction inside the multigrid V-cycle, through the C ABI:
-the network is trained on the GPU on pairs the solver generates, it lowers
-the error of the coarsest-level solve on fresh right-hand sides (what it
-gains at its own task), and the corrected preconditioner still gives
-converged FP64 solves, with no more iterations than the plain V-cycle."""
+"""Learned coarse correction inside the multigrid V-cycle, through the C ABI.
+
+The network is trained on the GPU on pairs the solver generates. The test
+checks three things:
+* the network lowers the error of a cheap coarsest-level solve (a degree-2
+  Chebyshev polynomial) on fresh right-hand sides, which is what it gains at
+  its own task;
+* the corrected preconditioner gives converged FP64 solves, with no more
+  iterations than the same cheap V-cycle without the network;
+* both reach the same solution.
+
+With the default degree-12 coarse polynomial, the coarsest solve of this
+hierarchy is already exact to FP32 rounding (relative error ~2e-9). There
+the network has nothing left to correct, and its residual input is rounding
+noise."""
 import numpy as np
 import pytest
 
@@ -21,12 +31,12 @@ def test_learned_coarse_correction(cuda):
     rng = np.random.default_rng(12)
     b = torch.tensor(rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof), device=cuda)
 
-    plain = Solver(op, pc="mg", precision="fp32", rtol=1e-10, maxit=200)
+    plain = Solver(op, pc="mg", precision="fp32", rtol=1e-10, maxit=200, mg_coarse_its=2)
     x0 = torch.zeros_like(b)
     its_plain, reason, _ = plain.solve(b, x0)
     assert reason > 0
 
-    s = Solver(op, pc="mg", precision="fp32", rtol=1e-10, maxit=200, mg_learned=True)
+    s = Solver(op, pc="mg", precision="fp32", rtol=1e-10, maxit=200, mg_coarse_its=2, mg_learned=True)
     loss = s.train_coarse(pairs=512, epochs=60, lr=1e-3, seed=3)
     assert np.isfinite(loss) and loss < 1.0
     e_plain, e_learned = s.coarse_gain(trials=16, seed=99)
