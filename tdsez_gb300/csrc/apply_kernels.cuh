@@ -68,8 +68,11 @@ __device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, 
 constexpr int kLoadsPerThread3 = 4;   // covers (TY+2p)(TX+2p) / (TX TY) for p <= 5
 
 // TX is the largest tile width; the launch may use a narrower one
-// (blockDim.x = 16..TX) to fit n0 with less padding.
-template <class T, int P, bool HB, bool HC, int TX, int TY>
+// (blockDim.x = 16..TX) to fit n0 with less padding. KA / KC: the kind of the
+// outer combinations fixed at compile time (0 complex, 1 real, 2 imaginary);
+// the double-float CN stage (KC = 2) and mass (KA = 1) get their own
+// instantiations, which save a quarter of the outer-stage products.
+template <class T, int P, bool HB, bool HC, int TX, int TY, int KA = 0, int KC = 0>
 __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     using C = typename CT<T>::type;
     constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
@@ -212,9 +215,16 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
 #pragma unroll
                 for (int o = 0; o < BW; ++o) {
                     C &a = acc[(ph - P + o + 2 * BW) % BW];
-                    kfma(a, zA[o], wA, prm.za_kind);
+                    if constexpr (KA == 1) rfma(a, zA[o].x, wA);
+                    else if constexpr (KA == 2) ifma(a, zA[o].y, wA);
+                    else cfma(a, zA[o], wA);
                     if constexpr (HB) rfma(a, sZM[(size_t)it * BW + o], wB);
-                    if constexpr (HC) kfma(a, sZC[(size_t)it * BW + o], wC, prm.zc_kind);
+                    if constexpr (HC) {
+                        const C zc = sZC[(size_t)it * BW + o];
+                        if constexpr (KC == 1) rfma(a, zc.x, wC);
+                        else if constexpr (KC == 2) ifma(a, zc.y, wC);
+                        else cfma(a, zc, wC);
+                    }
                 }
             }
             if (it >= 2 * P) {
@@ -374,12 +384,12 @@ inline int pick_tile_x(int n0) {
     return best;
 }
 
-template <class T, int P, bool HB, bool HC>
+template <class T, int P, bool HB, bool HC, int KA = 0, int KC = 0>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     using C = typename CT<T>::type;
     ApplyParams<T> prm = prm0;
     constexpr int TY = TileY<T, HB, HC>::v, NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
-    auto kern = k_apply3d<T, P, HB, HC, kTX3, TY>;
+    auto kern = k_apply3d<T, P, HB, HC, kTX3, TY, KA, KC>;
     // FP32 (HBM-leaning): full warps along x, about 8 CTAs per SM. FP64 and
     // double-float (FP64/FP32-pipe bound): the tile width with the least x
     // padding and the z chunking with the fewest waves x (chunk + halo).
@@ -428,6 +438,10 @@ inline void run2d(const ApplyParams<T> &prm0, cudaStream_t st) {
 template <class T, int P>
 inline void dispatch_streams(int dim, bool hb, bool hc, const ApplyParams<T> &prm, cudaStream_t st) {
     if (dim == 3) {
+        if constexpr (std::is_same<T, dff>::value) {
+            if (!hb && hc && prm.zc_kind == 2) { run3d<T, P, false, true, 0, 2>(prm, st); return; }   // CN stage
+            if (!hb && !hc && prm.za_kind == 1) { run3d<T, P, false, false, 1, 0>(prm, st); return; }  // mass
+        }
         if (hb && hc) run3d<T, P, true, true>(prm, st);
         else if (hb) run3d<T, P, true, false>(prm, st);
         else if (hc) run3d<T, P, false, true>(prm, st);
