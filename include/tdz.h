@@ -134,6 +134,22 @@ tdz_status tdz_operator_apply(tdz_op *op, int which, int precision, const void *
 /* x <- M^-1 x in place (exact Kronecker inverse of the overlap, banded
  * Cholesky line solves), FP32 or FP64 device vector. */
 tdz_status tdz_operator_mass_solve(tdz_op *op, int precision, void *x, void *stream);
+/* Launch-shape autotuning of the fused 3D apply: with on = 1 (the default)
+ * the first apply of each kernel variant and grid size times the candidate
+ * tile widths and z chunks on the caller's stream (CUDA events, about 30 ms
+ * once) and keeps the fastest; with on = 0 a fixed heuristic picks them. */
+void tdz_set_autotune(int on);
+/* Observables of a state (FP64 device vector psi) in one call: the monitor
+ * products of TDSEZManager::MonitorProducts (src/manager.cpp:584-672) reduced
+ * to expectation values. out (host, 2 + 2 + 2 dim doubles):
+ *   out[0]            <psi|M|psi>   (the norm; real)
+ *   out[1]            0
+ *   out[2], out[3]    <psi|H|psi>   (energy; complex with a CAP)
+ *   out[4 + 2a], +1   <psi|D_a|psi> (dipole along axis a; a < dim)
+ * The applies run in double-float arithmetic (TDZ_FP64_DF) and the
+ * reductions are the deterministic FP64 multi-dot; work buffers are allocated
+ * on the first call. Synchronises the stream (the values are returned). */
+tdz_status tdz_observables(tdz_op *op, const void *psi, double *out, void *stream);
 /* Number of fused-apply kernel launches issued so far by this operator. */
 long long tdz_operator_launches(const tdz_op *op);
 void tdz_operator_destroy(tdz_op *op);

@@ -277,6 +277,22 @@ tdz_status tdz_plane_transform(const double *B, int K, int N, const float *in, i
     });
 }
 
+void tdz_set_autotune(int on) { tdz::set_autotune(on); }
+
+tdz_status tdz_observables(tdz_op *op, const void *psi, double *out, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(op && psi && out, TDZ_ERR_ARG, "null argument");
+        std::vector<tdz::cd> v;
+        op->o.observables(static_cast<const double2 *>(psi), v, static_cast<cudaStream_t>(stream));
+        out[0] = v[0].real();
+        out[1] = 0.0;
+        for (size_t i = 1; i < v.size(); ++i) {
+            out[2 * i] = v[i].real();
+            out[2 * i + 1] = v[i].imag();
+        }
+    });
+}
+
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out) {
     return guarded([&] {
         TDZ_CHECK(op && out, TDZ_ERR_ARG, "null argument");

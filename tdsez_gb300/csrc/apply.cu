@@ -2,9 +2,33 @@
 // parameters, degree-specific instantiations in apply_p<P>.cu.
 #include "apply_kernels.cuh"
 
+#include <atomic>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 namespace tdz {
+
+namespace {
+std::atomic<int> g_autotune{1};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+}  // namespace
+
+bool autotune_enabled() { return g_autotune.load() != 0; }
+void set_autotune(int on) { g_autotune.store(on ? 1 : 0); }
+bool tune_lookup(const TuneKey &k, int *txw, int *zchunk) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(k);
+    if (it == g_tune.end()) return false;
+    *txw = it->second.first;
+    *zchunk = it->second.second;
+    return true;
+}
+void tune_store(const TuneKey &k, int txw, int zchunk) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[k] = {txw, zchunk};
+}
 
 namespace {
 

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <type_traits>
+#include <vector>
 
 #include "cplx.cuh"
 #include "oper.h"
@@ -384,46 +385,90 @@ inline int pick_tile_x(int n0) {
     return best;
 }
 
+// ---------------------------------------------------------------- autotuner
+// Launch shape (tile width, z chunk) of the 3D apply, chosen per kernel
+// instantiation and grid size by timing the candidates on the first launch
+// (CUDA events on the caller's stream, one warm-up and two timed launches
+// each, about 30 ms once for the double-float apply). Off: the heuristic
+// shape. Switched by tdz_set_autotune (default on).
+struct TuneKey {
+    const void *kern;
+    int n0, n1, n2;
+    bool operator<(const TuneKey &o) const {
+        if (kern != o.kern) return kern < o.kern;
+        if (n0 != o.n0) return n0 < o.n0;
+        if (n1 != o.n1) return n1 < o.n1;
+        return n2 < o.n2;
+    }
+};
+bool autotune_enabled();
+bool tune_lookup(const TuneKey &k, int *txw, int *zchunk);
+void tune_store(const TuneKey &k, int txw, int zchunk);
+
 template <class T, int P, bool HB, bool HC, int KA = 0, int KC = 0>
 inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     using C = typename CT<T>::type;
-    ApplyParams<T> prm = prm0;
     constexpr int TY = TileY<T, HB, HC>::v, NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
     auto kern = k_apply3d<T, P, HB, HC, kTX3, TY, KA, KC>;
-    // FP32 (HBM-leaning): full warps along x, about 8 CTAs per SM. FP64 and
-    // double-float (FP64/FP32-pipe bound): the tile width with the least x
-    // padding and the z chunking with the fewest waves x (chunk + halo).
     const bool fp32 = std::is_same<T, float>::value;
-    const int txw = fp32 ? kTX3 : pick_tile_x(prm.n0);
-    const int tiles = ((prm.n0 + txw - 1) / txw) * ((prm.n1 + TY - 1) / TY);
     const size_t tile_smem = sizeof(C) * ((size_t)(TY + 2 * P) * (kTX3 + 2 * P) + 2 * NU * (TY + 2 * P) * kTX3);
-    if (fp32) {
-        prm.zchunk = std::min(pick_chunk(tiles, prm.n2, P), 96);
-    } else {
-        static int slots = 0;   // resident CTAs on the GPU at the largest dynamic smem (96-plane chunks)
-        if (!slots) {
-            const size_t smax =
-                tile_smem + (size_t)(96 + 2 * P) * (2 * P + 1) * (sizeof(C) * (HC ? 2 : 1) + (HB ? sizeof(T) : 0));
-            TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-            int per_sm = 0, dev = 0, nsm = 0;
-            TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, txw * TY, smax));
-            TDZ_CUDA(cudaGetDevice(&dev));
-            TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-            slots = std::max(1, per_sm) * nsm;
+    auto smem_for = [&](int zchunk) {
+        const size_t rows = (size_t)(zchunk + 2 * P) * (2 * P + 1);
+        return tile_smem + rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
+    };
+    // one opt-in for the largest chunk, then occupancy at that size
+    static int slots = 0;
+    if (!slots) {
+        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(96)));
+        int per_sm = 0, dev = 0, nsm = 0;
+        TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTX3 * TY, smem_for(96)));
+        TDZ_CUDA(cudaGetDevice(&dev));
+        TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        slots = std::max(1, per_sm) * nsm;
+    }
+    auto tiles_for = [&](int txw) { return ((prm0.n0 + txw - 1) / txw) * ((prm0.n1 + TY - 1) / TY); };
+    auto launch = [&](int txw, int zchunk) {
+        ApplyParams<T> prm = prm0;
+        prm.zchunk = zchunk;
+        prm.zchunk_planes = zchunk + 2 * P;
+        dim3 grid(tiles_for(txw), (prm.n2 + zchunk - 1) / zchunk);
+        kern<<<grid, dim3(txw, TY), smem_for(zchunk), st>>>(prm);
+    };
+    // heuristic: FP32 (HBM-leaning) full warps along x and about 8 CTAs per SM;
+    // FP64 and double-float the least x padding and the fewest waves x (chunk + halo)
+    int txw = fp32 ? kTX3 : pick_tile_x(prm0.n0);
+    int zchunk = fp32 ? std::min(pick_chunk(tiles_for(txw), prm0.n2, P), 96)
+                      : std::min(pick_chunk_waves(tiles_for(txw), prm0.n2, P, slots), 96);
+    const TuneKey key{reinterpret_cast<const void *>(kern), prm0.n0, prm0.n1, prm0.n2};
+    if (autotune_enabled() && !tune_lookup(key, &txw, &zchunk)) {
+        std::vector<std::pair<int, int>> cand;
+        for (int t = kTX3; t >= 16; t -= 4) {
+            if ((prm0.n0 + t - 1) / t * t > (prm0.n0 + kTX3 - 1) / kTX3 * kTX3) continue;   // more padding than 32
+            const int tl = tiles_for(t);
+            for (int z : {std::min(pick_chunk(tl, prm0.n2, P), 96), std::min(pick_chunk_waves(tl, prm0.n2, P, slots), 96),
+                          std::min(pick_chunk_waves(tl, prm0.n2, P, 2 * slots), 96)})
+                if (std::find(cand.begin(), cand.end(), std::make_pair(t, z)) == cand.end()) cand.push_back({t, z});
         }
-        prm.zchunk = std::min(pick_chunk_waves(tiles, prm.n2, P, slots), 96);
+        cudaEvent_t e0, e1;
+        TDZ_CUDA(cudaEventCreate(&e0));
+        TDZ_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        for (const auto &c : cand) {
+            launch(c.first, c.second);
+            TDZ_CUDA(cudaEventRecord(e0, st));
+            launch(c.first, c.second);
+            launch(c.first, c.second);
+            TDZ_CUDA(cudaEventRecord(e1, st));
+            TDZ_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            TDZ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; txw = c.first; zchunk = c.second; }
+        }
+        TDZ_CUDA(cudaEventDestroy(e0));
+        TDZ_CUDA(cudaEventDestroy(e1));
+        tune_store(key, txw, zchunk);
     }
-    prm.zchunk_planes = prm.zchunk + 2 * P;
-    const size_t rows = (size_t)prm.zchunk_planes * (2 * P + 1);
-    const size_t smem = tile_smem + rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
-    // static + dynamic shared memory above 48 KB needs the opt-in (set once per size increase)
-    static size_t opted = 0;
-    if (smem > opted) {
-        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        opted = smem;
-    }
-    dim3 grid(tiles, (prm.n2 + prm.zchunk - 1) / prm.zchunk);
-    kern<<<grid, dim3(txw, TY), smem, st>>>(prm);
+    launch(txw, zchunk);
 }
 
 template <class T, int P, bool HB, bool HC>

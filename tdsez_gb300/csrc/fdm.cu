@@ -251,11 +251,11 @@ struct ZSolveParams {
 // per line, lines contiguous in memory (coalesced across the warp). The
 // recursion along z is latency-bound, so (1) the line matrix bands
 // A_z(s) = Bc + s Cc are evaluated once per CTA into shared memory, (2) the
-// right-hand side rows are prefetched 16 rows ahead into a register ring,
+// right-hand side rows are prefetched 32 rows ahead into a register ring,
 // and the back substitution prefetches its x and U rows 8 rows ahead, and
 // (3) the U scratch keeps the reciprocal pivot, so each row costs one complex
 // reciprocal. Shared memory: 2 n2 (2P+1) float2 (the two band combinations).
-constexpr int kZDist = 16, kZDistB = 8;
+constexpr int kZDist = 32, kZDistB = 8;
 
 template <int P>
 __global__ void __launch_bounds__(128) k_zsolve(const ZSolveParams prm) {

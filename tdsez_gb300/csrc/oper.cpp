@@ -16,6 +16,8 @@
 // changing the stage changes only scalars, never a band.
 #include "oper.h"
 
+#include "blas.h"
+
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -271,6 +273,27 @@ void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t s
         quad.apply(coef, prec, x, y, st);
     }
     ++launches;
+}
+
+void Operator::observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st) {
+    const int dim = sp->dim;
+    const size_t n = (size_t)sp->ndof();
+    const int k = 2 + dim;
+    if ((int)obs_buf.size() < k) {
+        obs_buf.clear();
+        for (int i = 0; i < k; ++i) obs_buf.emplace_back(n * sizeof(double2));
+    }
+    const int which[5] = {TDZ_MASS, TDZ_HAMILTONIAN, TDZ_DIPOLE_X, TDZ_DIPOLE_Y, TDZ_DIPOLE_Z};
+    std::vector<const void *> V(k);
+    for (int i = 0; i < k; ++i) {
+        apply(which[i], TDZ_FP64_DF, psi, obs_buf[i].ptr, st);
+        V[i] = obs_buf[i].ptr;
+    }
+    blas::Reducer red;
+    std::vector<cd> d(k);
+    blas::mdot(red, V.data(), k, psi, n, TDZ_FP64, d.data(), st);   // conj(A psi) . psi
+    out.resize(k);
+    for (int i = 0; i < k; ++i) out[i] = std::conj(d[i]);
 }
 
 }  // namespace tdz

@@ -75,10 +75,16 @@ struct Operator {
     void compile(Plan &pl, const std::vector<Term> &ts) const;
     void set_stage(cd alpha, cd g, const std::vector<cd> &c);
     void apply(int which, int prec, const void *x, void *y, cudaStream_t st);
+    // <psi|M|psi>, <psi|H|psi>, <psi|D_a|psi> (FP64 psi); see tdz_observables
+    std::vector<DevBuf> obs_buf;
+    void observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
 };
 
 // base band ids present on every axis
 enum BaseId { kM = 0, kS = 1, kX = 2 };
+
+// launch-shape autotuning of the 3D apply (apply.cu; on by default)
+void set_autotune(int on);
 
 // kernel launchers (apply.cu)
 void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st);

@@ -149,6 +149,15 @@ class Operator:
                                                   C.c_void_p(y.data_ptr()), C.c_void_p(s)))
         return y
 
+    def observables(self, psi, stream=None):
+        """(<psi|M|psi>, <psi|H|psi>, [<psi|D_a|psi>]) of a complex128 CUDA
+        state: the monitor expectation values of src/manager.cpp:584-672."""
+        import torch
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        out = (C.c_double * (4 + 2 * self.space.dim))()
+        _lib.check(_lib.load().tdz_observables(self.handle, C.c_void_p(psi.data_ptr()), out, C.c_void_p(s)))
+        return out[0], complex(out[2], out[3]), [complex(out[4 + 2 * a], out[5 + 2 * a]) for a in range(self.space.dim)]
+
     def mass_solve(self, x, stream=None):
         """x <- M^-1 x in place (complex64 / complex128 CUDA tensor)."""
         import torch

@@ -103,3 +103,24 @@ def test_vec_mdot(cuda):
                                 C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     ref = np.array([np.vdot(v.cpu().numpy(), w.cpu().numpy()) for v in V])
     assert np.abs(out.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max() + 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["3d_heterostructure", "2d_softcore", "3d_const_mass_cap"])
+def test_observables(cuda, name):
+    """Norm, energy and dipoles of a state in one call (the monitor
+    expectation values), against the oracle's assembled matrices: 1e-12."""
+    import torch
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    rng = np.random.default_rng(21)
+    psi = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    norm, energy, dip = op.observables(torch.tensor(psi, device=cuda))
+    ref_n = np.vdot(psi, A.M @ psi)
+    ref_e = np.vdot(psi, A.H_total() @ psi)
+    assert abs(norm - ref_n.real) <= 1e-12 * abs(ref_n)
+    assert abs(energy - ref_e) <= 1e-12 * abs(ref_e)
+    for a in range(S.dim):
+        ref_d = np.vdot(psi, A.D[a] @ psi)
+        assert abs(dip[a] - ref_d) <= 1e-12 * max(abs(ref_d), 1e-3 * abs(ref_n)), (a, dip[a], ref_d)
