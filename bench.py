@@ -157,8 +157,8 @@ def run_tdz(args):
 
     # ---- headline arm: FP64 FGMRES, FP32 preconditioner (fast diagonalisation)
     t_setup = time.time()
-    G = Propagator(op, "cn", field=w.field, precision="fp32", pc=args.pc, rtol=RTOL, outer=args.outer,
-                   guess_order=args.guess_order)
+    G = Propagator(op, "cn", field=w.field, precision="fp32", pc=args.pc, rtol=args.rtol, outer=args.outer,
+                   guess_order=args.guess_order, relaxed=args.relaxed == "on")
     t_setup = time.time() - t_setup
     psi = psi0.clone()
     t = 0.0
@@ -251,9 +251,9 @@ def run_tdz(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 FGMRES) + c64 (FP32 multigrid)",
         "data": "synthetic (seeded heterostructure, Gaussian packet)",
         "config": {"workload": "3D heterostructure CN, 160x160x320 el, p=3, 5 C0 interfaces, N=%d" % N,
-                   "global_batch": world, "dt": dt, "rtol": RTOL, "precond": args.pc + " (FP32) in FP64 FGMRES",
+                   "global_batch": world, "dt": dt, "rtol": args.rtol, "precond": args.pc + " (FP32) in FP64 FGMRES",
                    "outer_apply": {"df": "double-float (FP32 pairs)", "fp64": "native FP64"}[args.outer],
-                   "guess_order": args.guess_order,
+                   "guess_order": args.guess_order, "relaxed_arnoldi": args.relaxed,
                    "mg": {"smooth": args.mg_smooth, "coarse_its": args.mg_coarse_its, "levels": args.mg_levels},
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "working set > L2 (state alone 141.6 MB)"},
@@ -367,6 +367,8 @@ def main():
     ap.add_argument("--pc", default="fdm")
     ap.add_argument("--outer", default="df", choices=["df", "fp64"])
     ap.add_argument("--guess-order", type=int, default=3)
+    ap.add_argument("--rtol", type=float, default=RTOL)
+    ap.add_argument("--relaxed", default="off", choices=["on", "off"])
     ap.add_argument("--apply-only", action="store_true")
     ap.add_argument("--precond-only", action="store_true")
     ap.add_argument("--mg-smooth", type=int, default=8)

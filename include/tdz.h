@@ -184,6 +184,12 @@ typedef struct tdz_solver_opts {
     int mg_learned;     /* 1 = learned CNN correction of the coarsest solve
                            (TDZ_PC_MG with FP32 levels; active once trained by
                            tdz_solver_train_coarse)                          */
+    int relaxed;        /* 1 = relaxed (inexact) Krylov: the Arnoldi applies
+                           A z_j in FP32; the residual b - A x of every
+                           restart in outer_precision, and a cycle that
+                           reports convergence is confirmed by one more such
+                           residual (the returned rnorm is that true
+                           residual)                                         */
 } tdz_solver_opts;
 /* Set up the solver for the current stage of op (call set_stage first). */
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);
@@ -246,7 +252,7 @@ tdz_status tdz_vec_mdot_noalloc(const void *const *V, int k, const void *w, long
                                 void *stream);
 
 /* Batched complex-by-real transform on the tensor cores (tcgen05, TF32 with
- * a three-term split: FP32-class accuracy), the eigenvector transform of the
+ * a hi/lo split of both operands: FP32 accuracy), the eigenvector transform of the
  * fast-diagonalisation preconditioner; the counterpart of the per-axis
  * contraction of TDSEZTensorOps::Term (src/tensorops.cpp:97-153) for a dense
  * matrix:

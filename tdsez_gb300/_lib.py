@@ -53,6 +53,7 @@ class tdz_solver_opts(C.Structure):
         ("mg_coarse_its", C.c_int),
         ("outer_precision", C.c_int),
         ("mg_learned", C.c_int),
+        ("relaxed", C.c_int),
     ]
 
 

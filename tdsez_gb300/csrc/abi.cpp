@@ -258,6 +258,7 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     so.mg.coarse_its = o->mg_coarse_its > 0 ? o->mg_coarse_its : 12;
     so.outer = o->outer_precision == 0 ? TDZ_FP64 : o->outer_precision;
     so.mg.learned = o->mg_learned;
+    so.relaxed = o->relaxed != 0;
     TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
               "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;

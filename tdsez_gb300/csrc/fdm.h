@@ -28,7 +28,7 @@ struct PcFDM : Precond {
     DevBuf zb;                 // FP32 outer base bands (a copy of the operator's)
     DevBuf b1, b2, ufac;       // FP32 work vectors and the U factors of the line solves
     bool exact = true;         // false: inner one-axis terms other than stiffness were dropped
-    // 3D with n_x, n_y <= 256: transforms on the tensor cores (tcgen05, TF32 x 3) over
+    // 3D with n_x, n_y <= 256: transforms on the tensor cores (tcgen05, TF32 hi/lo split) over
     // row-planar FP32 buffers pa ([z][y][c][x], pitch ldx) and pb ([z][x][c][y], pitch ldy)
     bool tensor = false;
     TransformMat Tf[2], Ti[2];

@@ -19,6 +19,10 @@ void FGMRES::setup(Operator *op_, int restart_, Precond *pc_) {
     for (int i = 0; i <= restart; ++i) V.emplace_back(n * sizeof(double2));
     for (int i = 0; i < restart; ++i) Z.emplace_back(n * sizeof(double2));
     w.alloc(n * sizeof(double2));
+    if (relaxed) {
+        z32.alloc(n * sizeof(float2));
+        w32.alloc(n * sizeof(float2));
+    }
     red.init();
 }
 
@@ -45,6 +49,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     for (int i = 0; i <= m; ++i) Vp[i] = V[i].ptr;
     for (int i = 0; i < m; ++i) Zp[i] = Z[i].ptr;
     int total = 0;
+    bool used_relaxed = false;
     while (true) {
         // r = b - A x  -> V0
         double2 *v0 = V[0].as<double2>();
@@ -66,7 +71,15 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             double2 *zj = Z[j].as<double2>();
             pc->apply(V[j].as<double2>(), zj, st);
             double2 *wv = w.as<double2>();
-            op->apply(TDZ_STAGE, aprec, zj, wv, st);
+            if (relaxed) {
+                blas::cast(zj, TDZ_FP64, z32.ptr, TDZ_FP32, n, st);
+                op->apply(TDZ_STAGE, TDZ_FP32, z32.ptr, w32.ptr, st);
+                blas::cast(w32.ptr, TDZ_FP32, wv, TDZ_FP64, n, st);
+                ++relaxed_applies;
+                used_relaxed = true;
+            } else {
+                op->apply(TDZ_STAGE, aprec, zj, wv, st);
+            }
             ++applies;
             // CGS with one re-orthogonalisation; up to 16 basis vectors the
             // update and the next reduction share one pass over V and w
@@ -118,7 +131,12 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         }
         if (k > 0) blas::maxpy(x, k, Zp.data(), y.data(), n, TDZ_FP64, st);
         if (s.reason == -9) break;
-        if (done && s.rnorm <= target) { s.reason = 2; break; }
+        if (done && s.rnorm <= target) {
+            // relaxed applies: the restart computes the true residual and decides
+            if (used_relaxed) { used_relaxed = false; continue; }
+            s.reason = 2;
+            break;
+        }
         if (done) continue;            // happy breakdown without meeting the target: restart
         if (total >= maxit) { s.reason = -3; break; }
     }

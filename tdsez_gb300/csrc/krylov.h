@@ -46,6 +46,13 @@ struct FGMRES {
     SolveStats last;
     long long applies = 0;
     int aprec = TDZ_FP64;   // operator apply arithmetic: TDZ_FP64 or TDZ_FP64_DF (FP64 vectors either way)
+    // Relaxed Arnoldi applies (inexact Krylov): A z_j in FP32 while the
+    // residual r0 = b - A x of every restart stays in aprec. A cycle that
+    // reports convergence is followed by one more restart, whose aprec
+    // residual decides; the result is therefore judged on the true residual.
+    bool relaxed = false;
+    DevBuf z32, w32;
+    long long relaxed_applies = 0;
 
     void setup(Operator *op_, int restart_, Precond *pc_);
     // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.

@@ -63,6 +63,7 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
         p->setup(op);
         pc = std::move(p);
     } else throw Error(TDZ_ERR_ARG, "unknown preconditioner");
+    ksp.relaxed = o.relaxed;
     ksp.setup(op, restart, pc.get());
     TDZ_CHECK(o.outer == TDZ_FP64 || o.outer == TDZ_FP64_DF, TDZ_ERR_ARG, "outer precision must be FP64 or FP64_DF");
     ksp.aprec = o.outer;

@@ -17,6 +17,7 @@ struct SolverOptions {
     int pc = 2;           // 0 none, 1 Kronecker mass, 2 multigrid
     int pc_precision = TDZ_FP32;
     int outer = TDZ_FP64;  // operator applies of FGMRES and the right-hand sides (TDZ_FP64 or TDZ_FP64_DF)
+    bool relaxed = false;  // FP32 Arnoldi applies, true residual in `outer` at every restart
     MGOptions mg;
 };
 

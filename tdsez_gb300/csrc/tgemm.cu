@@ -11,10 +11,11 @@
 //   stage = A (128 x 32 FP32, split by warps 0-3 in place into TF32 hi, with
 //           the lo part in one of two extra buffers; both rounded to nearest)
 //         + B hi, B lo (Np x 32 each, split on the host).
-// Per 8-wide K step thread 0 issues three MMAs,
-//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi,
-// which keeps about 22 significant bits (the dropped A_lo B_lo term is
-// ~2^-22 relative): FP32-class results at TF32 tensor-core rates. At the end
+// Per 8-wide K step thread 0 issues four MMAs,
+//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi + A_lo B_lo,
+// the full product of the hi/lo splits (each part rounded to TF32), so the
+// result has FP32 accuracy at TF32 tensor-core rates (the transform is bound
+// by its loads, not by the tensor pipe). At the end
 // of a tile warps 0-3 read TMEM with tcgen05.ld (warp w owns lanes
 // 32w..32w+31, lane = tile row) and store the tile transposed per plane.
 // Every wait on an mbarrier is bounded (clock64): on time-out the kernel sets
@@ -253,6 +254,7 @@ __global__ void __launch_bounds__(160, 1)
                         mma_tf32(d, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
                         mma_tf32(d, dah, dbl, idesc, 1u);
                         mma_tf32(d, dal, dbh, idesc, 1u);
+                        mma_tf32(d, dal, dbl, idesc, 1u);
                     }
                 }
                 mma_commit(done0 + 8 * s);

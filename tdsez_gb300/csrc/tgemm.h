@@ -1,5 +1,5 @@
 // Batched complex-by-real transforms on the 5th-generation tensor cores
-// (tcgen05, TF32 with a three-term split, FP32-class accuracy). Internal.
+// (tcgen05, TF32 with a hi/lo split of both operands, FP32 accuracy). Internal.
 //
 //   out[p][n][c][r] = sum_k in[p][r][c][k] B[k][n]      (p < planes, r < R, c = re/im)
 //

@@ -25,7 +25,7 @@ MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 
 def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
                 maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 0, mg_coarse_its: int = 12,
-                outer: str = "fp64", mg_learned: bool = False):
+                outer: str = "fp64", mg_learned: bool = False, relaxed: bool = False):
     """Solver options. ``precision`` is the preconditioner's arithmetic
     (fp32 = mixed precision); ``outer`` the arithmetic of the FP64 Krylov
     method's operator applies: "fp64" (native) or "df" (double-float on the
@@ -41,6 +41,7 @@ def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, re
     o.mg_coarse_its = mg_coarse_its
     o.outer_precision = {"fp64": _lib.TDZ_FP64, "df": _lib.TDZ_FP64_DF}[outer]
     o.mg_learned = 1 if mg_learned else 0
+    o.relaxed = 1 if relaxed else 0
     return o
 
 

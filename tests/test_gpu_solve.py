@@ -183,3 +183,33 @@ def test_failed_solve_is_a_status(cuda):
     # the library stays usable afterwards
     psi = torch.randn(PS.ndof, dtype=torch.complex128, device=cuda)
     G2.step(psi, 0.0, 0.5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["3d_heterostructure", "3d_softcore", "2d_cap_softcore_sep"])
+@pytest.mark.parametrize("pc", ["fdm", "mg"])
+def test_relaxed_arnoldi_solve(cuda, name, pc):
+    """Relaxed (inexact) Krylov: Arnoldi applies in FP32, every restart
+    residual in double-float. The answer is still the FP64 solution: true
+    residual of the oracle matrix <= 1e-11, and the reported residual is a
+    true one."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    tau = 0.2
+    cc = [0.02 * (k + 1) for k in range(len(c["coupled"]))]
+    op.set_stage(1.0, 1j * tau, cc)
+    Am = (A.M + 1j * tau * (A.H_total() + sum(ck * T for ck, T in zip(cc, A.terms())))).tocsc()
+    rng = np.random.default_rng(31)
+    b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    s = Solver(op, pc=pc, precision="fp32", rtol=1e-12, maxit=400, outer="df", relaxed=True)
+    bd = torch.tensor(b, device=cuda)
+    xd = torch.zeros_like(bd)
+    its, reason, rn = s.solve(bd, xd)
+    x = xd.cpu().numpy()
+    assert reason > 0, (its, reason, rn)
+    rres = np.linalg.norm(b - Am @ x) / np.linalg.norm(b)
+    assert rres < 1e-11 or _berr(Am, x, b) < 1e-13, (rres, _berr(Am, x, b))
+    assert rn <= 1e-12 * np.linalg.norm(b) * 1.0001

@@ -1,4 +1,4 @@
-"""Tensor-core plane transform (tcgen05, TF32 with a three-term split)
+"""Tensor-core plane transform (tcgen05, TF32 with a hi/lo split of both operands)
 against numpy FP64, through the C ABI. Bar: FP32 class, i.e. a max-norm
 relative error at most 4x that of the same contraction evaluated in FP32 by
 numpy (about 1e-6 at K = 163), and never above 1e-5."""
