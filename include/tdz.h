@@ -278,11 +278,27 @@ typedef struct tdz_prop tdz_prop;
 #define TDZ_CN 0
 #define TDZ_PADE22 1
 #define TDZ_MAGNUS4 2
+/* guess_order: 0..5, the initial guess of each stage solve extrapolated from
+ * the previous steps (-pade_guess_order, src/propagator.cpp:634-637); -1,
+ * the preconditioner's answer x0 = P^-1 b (with the exact FDM inverse this
+ * leaves a residual near FP32 rounding, and one FGMRES iteration ends the
+ * solve). */
 tdz_status tdz_prop_create(tdz_op *op, int kind, const tdz_solver_opts *opts, int guess_order, void *stream,
                            tdz_prop **out);
 tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, const double *c2, void *stream);
 /* Totals: stage solves, Krylov iterations, FP64 operator applies of the
  * solver, multigrid cycles; last solve's iterations and relative residual. */
+/* Batched steps: count independent propagations (each its own tdz_prop, psi,
+ * field coefficients c1[i] / c2[i] and stream streams[i]; grids, degrees and
+ * physics may differ) advanced by one step h each, concurrently. Host threads
+ * (threads; 0 = 16) take the runs from a shared counter and step them on
+ * their own streams, so the GPU overlaps the small kernels and host
+ * synchronisations of many runs, for intensity and phase scans. Returns the
+ * first failure (tdz_last_error names the run); the other runs still step.
+ * No counterpart in the reference (one propagation per process there). */
+tdz_status tdz_prop_step_batch(int count, tdz_prop *const *props, void *const *psis, double h,
+                               const double *const *c1, const double *const *c2, void *const *streams, int threads);
+
 tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies,
                           long long *cycles, int *last_its, double *last_rres);
 void tdz_prop_destroy(tdz_prop *p);

@@ -121,6 +121,8 @@ SIGNATURES = {
     "tdz_solver_train_coarse": (I, [VP, I, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), VP]),
     "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
     "tdz_set_autotune": (None, [I]),
+    "tdz_prop_step_batch": (I, [I, C.POINTER(VP), C.POINTER(VP), C.c_double, C.POINTER(C.POINTER(C.c_double)),
+                                C.POINTER(C.POINTER(C.c_double)), C.POINTER(VP), I]),
     "tdz_observables": (I, [VP, VP, C.POINTER(C.c_double), VP]),
     "tdz_plane_transform": (I, [C.POINTER(C.c_double), I, I, VP, I, I, I, VP, I, VP]),
     "tdz_cnn_create": (I, [I, I, I, I, I, I, I, I, C.c_ulonglong, PP]),

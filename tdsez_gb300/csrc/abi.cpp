@@ -9,6 +9,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 
 #include "oper.h"
 #include "prop.h"
@@ -389,6 +390,40 @@ tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, con
         else if (p->p.kind == TDZ_PADE22) p->p.pade_step(v, h, a, 0, st);
         else p->p.magnus_step(v, h, a, b, st);
     });
+}
+
+tdz_status tdz_prop_step_batch(int count, tdz_prop *const *props, void *const *psis, double h,
+                               const double *const *c1, const double *const *c2, void *const *streams, int threads) {
+    if (count < 0 || (count > 0 && (!props || !psis || !streams))) {
+        tdz::set_last_error("bad batch arguments");
+        return TDZ_ERR_ARG;
+    }
+    const int nt = std::max(1, std::min(threads > 0 ? threads : 16, std::max(count, 1)));
+    std::atomic<int> next{0};
+    std::mutex mu;
+    tdz_status first = TDZ_OK;
+    std::string first_msg;
+    auto worker = [&]() {
+        while (true) {
+            const int i = next.fetch_add(1);
+            if (i >= count) break;
+            const tdz_status s = tdz_prop_step(props[i], psis[i], h, c1 ? c1[i] : nullptr, c2 ? c2[i] : nullptr,
+                                               streams[i]);
+            if (s != TDZ_OK) {
+                std::lock_guard<std::mutex> lk(mu);
+                if (first == TDZ_OK) {
+                    first = s;
+                    first_msg = "batch run " + std::to_string(i) + ": " + tdz_last_error();
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int k = 1; k < nt; ++k) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+    if (first != TDZ_OK) tdz::set_last_error(first_msg);
+    return first;
 }
 
 tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies, long long *cycles,

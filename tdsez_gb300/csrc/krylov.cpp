@@ -49,7 +49,8 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     for (int i = 0; i <= m; ++i) Vp[i] = V[i].ptr;
     for (int i = 0; i < m; ++i) Zp[i] = Z[i].ptr;
     int total = 0;
-    bool used_relaxed = false;
+    bool used_relaxed = false, relax = relaxed;
+    double beta_prev = -1.0;
     while (true) {
         // r = b - A x  -> V0
         double2 *v0 = V[0].as<double2>();
@@ -60,6 +61,11 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         if (!std::isfinite(beta)) { s.reason = -9; s.rnorm = beta; break; }
         s.rnorm = beta;
         if (beta <= target) { s.reason = 2; break; }
+        // a relaxed cycle that did not cut the true residual tenfold: the FP32
+        // applies limit the progress (ill-conditioned system); continue exactly
+        if (used_relaxed && beta_prev > 0.0 && beta > 0.1 * beta_prev) relax = false;
+        used_relaxed = false;
+        beta_prev = beta;
         if (total >= maxit) { s.reason = -3; break; }
         blas::scale(v0, 1.0 / beta, n, TDZ_FP64, st);
         std::fill(g.begin(), g.end(), cd(0));
@@ -71,7 +77,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             double2 *zj = Z[j].as<double2>();
             pc->apply(V[j].as<double2>(), zj, st);
             double2 *wv = w.as<double2>();
-            if (relaxed) {
+            if (relax) {
                 blas::cast(zj, TDZ_FP64, z32.ptr, TDZ_FP32, n, st);
                 op->apply(TDZ_STAGE, TDZ_FP32, z32.ptr, w32.ptr, st);
                 blas::cast(w32.ptr, TDZ_FP32, wv, TDZ_FP64, n, st);
@@ -133,7 +139,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         if (s.reason == -9) break;
         if (done && s.rnorm <= target) {
             // relaxed applies: the restart computes the true residual and decides
-            if (used_relaxed) { used_relaxed = false; continue; }
+            if (used_relaxed) continue;
             s.reason = 2;
             break;
         }

@@ -82,7 +82,7 @@ void Propagator::setup(Operator *op_, int kind_, const SolverOptions &o, int gue
     op = op_;
     kind = kind_;
     TDZ_CHECK(kind >= 0 && kind <= 2, TDZ_ERR_ARG, "unknown propagator kind");
-    TDZ_CHECK(guess_order_ >= 0 && guess_order_ <= 5, TDZ_ERR_ARG, "guess order must be 0..5");
+    TDZ_CHECK(guess_order_ >= -1 && guess_order_ <= 5, TDZ_ERR_ARG, "guess order must be -1..5");
     guess_order = guess_order_;
     n = (size_t)op->sp->ndof();
     rhs.alloc(n * sizeof(double2));
@@ -136,8 +136,12 @@ void Propagator::cn_step(double2 *psi, double h, const std::vector<cd> &c, cudaS
     op->set_stage(1.0, cd(0.0, 0.5 * h), c);
     op->apply(TDZ_MASS, aprec, psi, rhs.ptr, st);          // M psi
     double2 *X = tmp.as<double2>();
-    blas::copy(psi, X, n, TDZ_FP64, st);
-    extrapolate(0, X, st);
+    if (guess_order < 0) {
+        solver[0].pc->apply(rhs.as<double2>(), X, st);           // x0 = P^-1 b
+    } else {
+        blas::copy(psi, X, n, TDZ_FP64, st);
+        extrapolate(0, X, st);
+    }
     stage_solve(0, rhs.as<double2>(), X, st);
     record(0, X, psi, st);
     blas::axpby(psi, 2.0, X, -1.0, n, TDZ_FP64, st);           // psi <- 2 X - psi
@@ -154,8 +158,9 @@ void Propagator::pade_step(double2 *psi, double h, const std::vector<cd> &c, int
         blas::axpby(rhs.ptr, -1.0, tmp.ptr, 2.0, n, TDZ_FP64, st);
         blas::copy(psi, x0.ptr, n, TDZ_FP64, st);               // stage input
         const int s = 2 * slot + k;
-        extrapolate(s, psi, st);
         op->set_stage(1.0, g[k], c);
+        if (guess_order < 0) solver[k].pc->apply(rhs.as<double2>(), psi, st);   // x0 = P^-1 b
+        else extrapolate(s, psi, st);
         stage_solve(k, rhs.as<double2>(), psi, st);
         record(s, psi, x0.as<double2>(), st);
     }

@@ -110,6 +110,10 @@ class Propagator:
 
     def __init__(self, op: Operator, kind: str = "cn", field: Optional[Callable[[float], Sequence[float]]] = None,
                  guess_order: int = 3, stream=None, **kw):
+        """guess_order: 0..5 extrapolates the stage solutions of the previous
+        steps (-pade_guess_order); -1 starts each stage solve from the
+        preconditioner's answer x0 = P^-1 b (one FGMRES iteration per solve
+        with the exact FDM inverse)."""
         self.op = op
         self.kind = kind
         self.field = field or (lambda t: [0.0] * len(op.coupled))
@@ -170,3 +174,46 @@ class Propagator:
             except Exception:
                 pass
             self.handle = None
+
+
+class BatchPropagator:
+    """Many independent propagations advanced together (intensity / phase
+    scans): each run has its own Propagator, state and CUDA stream; one call
+    per step (``tdz_prop_step_batch``) steps them concurrently from a pool of
+    host threads, so the GPU overlaps the runs' small kernels and host
+    synchronisations. Runs may differ in grid, degree, physics and field."""
+
+    def __init__(self, props: Sequence[Propagator], threads: int = 16):
+        import torch
+        self.props = list(props)
+        if len({id(P.op) for P in self.props}) != len(self.props):
+            raise ValueError("each run needs its own Operator (the stage coefficients live there)")
+        self.threads = threads
+        self.streams = [torch.cuda.Stream() for _ in self.props]
+
+    def step(self, psis, t: float, h: float):
+        """One step from t to t + h of every run (psis[i]: complex128 CUDA tensors, in place)."""
+        import torch
+        n = len(self.props)
+        for s in self.streams:   # the states were written on the current stream
+            s.wait_stream(torch.cuda.current_stream())
+        c1s, c2s, keep = [], [], []
+        for P in self.props:
+            nc = len(P.op.coupled)
+            arr = C.c_double * max(1, nc)
+            if P.kind == "magnus4":
+                a = arr(*P.coeffs(t + MAGNUS_C[0] * h))
+                b = arr(*P.coeffs(t + MAGNUS_C[1] * h))
+            else:
+                a, b = arr(*P.coeffs(t + 0.5 * h)), arr(*([0.0] * max(1, nc)))
+            keep += [a, b]
+            c1s.append(C.cast(a, C.POINTER(C.c_double)))
+            c2s.append(C.cast(b, C.POINTER(C.c_double)))
+        VPA = C.c_void_p * n
+        DPA = C.POINTER(C.c_double) * n
+        _lib.check(_lib.load().tdz_prop_step_batch(
+            n, VPA(*[P.handle.value for P in self.props]), VPA(*[p.data_ptr() for p in psis]), h,
+            DPA(*c1s), DPA(*c2s), VPA(*[s.cuda_stream for s in self.streams]), self.threads))
+        for s in self.streams:
+            torch.cuda.current_stream().wait_stream(s)
+        return psis
