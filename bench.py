@@ -127,6 +127,74 @@ def time_kernel(fn, reps, stream):
     return s.elapsed_time(e) / 1e3 / reps
 
 
+def batch_scan(args):
+    """Intensity / carrier-envelope-phase scan of independent 2D soft-core
+    runs (V = -1/sqrt(x^2 + y^2 + 1) on [-100, 100]^2, field along x, CN
+    dt = 0.05): grids and degrees drawn per run with the seeded generator,
+    E0 log-uniform in [0.01, 0.1], CEP uniform in [0, 2 pi). The runs are
+    stepped one after another, then together (BatchPropagator: own streams,
+    host thread pool); reported as run-steps per second."""
+    import math as _m
+    import numpy as np
+    import torch
+    from tdsez_gb300 import _lib
+    from tdsez_gb300.operators import Operator, Physics
+    from tdsez_gb300.propagator import BatchPropagator, Propagator
+    from tdsez_gb300.space import Space, uniform_knots
+    torch.cuda.set_device(0)
+    _lib.load()
+    rng = np.random.default_rng(20261203)
+    T = 4 * 2 * _m.pi / 0.057
+    runs = []
+    for r in range(args.batch_scan):
+        nel = int(rng.integers(args.scan_min_el, args.scan_max_el + 1))
+        p = int(rng.integers(3, 6))
+        E0 = 10 ** rng.uniform(-2, -1)
+        phi = rng.uniform(0, 2 * _m.pi)
+        S = Space([uniform_knots(nel, -100.0, 100.0, p)] * 2, p, p + 1)
+        ph = Physics(charge=-1.0, mass=1.0, coupled=(0,), softcore=[(1.0, 0.0, 0.0, 0.0, 1.0)])
+        op = Operator(S, ph)
+        field = (lambda E0, phi: (lambda t: [E0 * _m.sin(_m.pi * t / T) ** 2 * _m.sin(0.057 * t + phi)]))(E0, phi)
+        psi = op.separable_state([lambda x: _m.exp(-x * x / 2.0)] * 2)
+        runs.append((S, op, field, psi, nel, p))
+    def make():
+        return [Propagator(op, "cn", field=f, pc="mg", precision="fp32", rtol=1e-10, outer="df")
+                for (S, op, f, psi, nel, p) in runs]
+    dt = 0.05
+    steps = args.steps
+    # serial
+    Ps = make()
+    st = [r[3].clone() for r in runs]
+    for G, x in zip(Ps, st):
+        G.step(x, 0.0, dt)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for k in range(1, steps + 1):
+        for G, x in zip(Ps, st):
+            G.step(x, k * dt, dt)
+    torch.cuda.synchronize()
+    t_serial = time.time() - t0
+    # batched
+    Pb = make()
+    B = BatchPropagator(Pb, threads=args.scan_threads)
+    sb = [r[3].clone() for r in runs]
+    B.step(sb, 0.0, dt)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for k in range(1, steps + 1):
+        B.step(sb, k * dt, dt)
+    torch.cuda.synchronize()
+    t_batch = time.time() - t0
+    n = len(runs)
+    print(json.dumps({"metric": "batched 2D soft-core scan, CN run-steps/s", "value": n * steps / t_batch,
+                      "unit": "run-steps/s", "serial": n * steps / t_serial, "speedup": t_serial / t_batch,
+                      "runs": n, "steps": steps, "threads": args.scan_threads,
+                      "grids": sorted(set(int(r[4]) for r in runs)), "degrees": sorted(set(int(r[5]) for r in runs)),
+                      "ndof_total": int(sum(r[0].ndof for r in runs)),
+                      "note": "host wall clock around K steps after one warm-up step; grids drawn in "
+                              "[%d, %d]^2 elements" % (args.scan_min_el, args.scan_max_el)}))
+
+
 def run_tdz(args):
     import torch
     from tdsez_gb300 import _lib, build as _build
@@ -366,11 +434,15 @@ def main():
     ap.add_argument("--mg-steps", type=int, default=2)
     ap.add_argument("--pc", default="fdm")
     ap.add_argument("--outer", default="df", choices=["df", "fp64"])
-    ap.add_argument("--guess-order", type=int, default=3)
+    ap.add_argument("--guess-order", type=int, default=-1)
     ap.add_argument("--rtol", type=float, default=RTOL)
     ap.add_argument("--relaxed", default="off", choices=["on", "off"])
     ap.add_argument("--apply-only", action="store_true")
     ap.add_argument("--precond-only", action="store_true")
+    ap.add_argument("--batch-scan", type=int, default=0, help="runs of the batched 2D scan (0: headline bench)")
+    ap.add_argument("--scan-min-el", type=int, default=128)
+    ap.add_argument("--scan-max-el", type=int, default=512)
+    ap.add_argument("--scan-threads", type=int, default=16)
     ap.add_argument("--mg-smooth", type=int, default=8)
     ap.add_argument("--mg-coarse-its", type=int, default=12)
     ap.add_argument("--mg-levels", type=int, default=0)
@@ -379,6 +451,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.batch_scan > 0:
+        batch_scan(args)
     else:
         run_tdz(args)
 

@@ -43,8 +43,10 @@ def test_batch_equals_serial(cuda):
             G.step(p, step * dt, dt)
         B.step(psis, step * dt, dt)
     torch.cuda.synchronize()
+    # the soft-core quadrature term adds element contributions with atomics, whose
+    # order differs between two executions: agreement to rounding, not bit for bit
     for (Gs, ps), pb in zip(serial, psis):
         a, b = ps.cpu().numpy(), pb.cpu().numpy()
-        assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(a)
+        assert np.linalg.norm(a - b) <= 1e-10 * np.linalg.norm(a)
     for G, _ in batch:
         assert G.stats()["solves"] == 3
