@@ -155,7 +155,7 @@ def batch_scan(args):
         ph = Physics(charge=-1.0, mass=1.0, coupled=(0,), softcore=[(1.0, 0.0, 0.0, 0.0, 1.0)])
         op = Operator(S, ph)
         field = (lambda E0, phi: (lambda t: [E0 * _m.sin(_m.pi * t / T) ** 2 * _m.sin(0.057 * t + phi)]))(E0, phi)
-        psi = op.separable_state([lambda x: _m.exp(-x * x / 2.0)] * 2)
+        psi = op.separable_state([lambda x: np.exp(-x * x / 2.0)] * 2)
         runs.append((S, op, field, psi, nel, p))
     def make():
         return [Propagator(op, "cn", field=f, pc="mg", precision="fp32", rtol=1e-10, outer="df")

@@ -185,11 +185,13 @@ typedef struct tdz_solver_opts {
                            (TDZ_PC_MG with FP32 levels; active once trained by
                            tdz_solver_train_coarse)                          */
     int relaxed;        /* 1 = relaxed (inexact) Krylov: the Arnoldi applies
-                           A z_j in FP32; the residual b - A x of every
-                           restart in outer_precision, and a cycle that
-                           reports convergence is confirmed by one more such
-                           residual (the returned rnorm is that true
-                           residual)                                         */
+                           A z_j in FP32, the residual b - A x of every
+                           restart in outer_precision. A cycle that reports
+                           convergence is accepted when the estimate plus
+                           the bound sum_j |y_j| 1e-4 ||A z_j|| on its gap
+                           to the true residual meets rtol (rnorm returns
+                           that sum), else one more restart residual
+                           decides                                           */
 } tdz_solver_opts;
 /* Set up the solver for the current stage of op (call set_stage first). */
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);

@@ -9,6 +9,10 @@
 
 namespace tdz {
 
+namespace {
+constexpr double kRelaxEps = 1e-4;   // bound on the relative error of an FP32 apply (measured: ~1e-6)
+}
+
 void FGMRES::setup(Operator *op_, int restart_, Precond *pc_) {
     op = op_;
     n = (size_t)op->sp->ndof();
@@ -45,6 +49,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     }
     const double target = rtol * bnorm;
     std::vector<cd> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), h(m + 1), h2(m + 1), y(m);
+    std::vector<double> wn(m, 0.0);     // ||A z_j|| of relaxed columns (0 for exact ones)
     std::vector<const void *> Vp(m + 1), Zp(m);
     for (int i = 0; i <= m; ++i) Vp[i] = V[i].ptr;
     for (int i = 0; i < m; ++i) Zp[i] = Z[i].ptr;
@@ -105,6 +110,12 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             }
             for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = -(h[i] + h2[i]);
             if (!std::isfinite(hn)) { s.reason = -9; done = true; break; }
+            wn[j] = 0.0;
+            if (relax) {   // ||A z_j||^2 = sum_i |H_ij|^2 + hn^2 (orthonormal V)
+                double q = hn * hn;
+                for (int i = 0; i <= j; ++i) q += std::norm(H[(size_t)i * m + j]);
+                wn[j] = std::sqrt(q);
+            }
             H[(size_t)(j + 1) * m + j] = hn;
             // apply previous rotations to column j
             for (int i = 0; i < j; ++i) {
@@ -138,8 +149,17 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         if (k > 0) blas::maxpy(x, k, Zp.data(), y.data(), n, TDZ_FP64, st);
         if (s.reason == -9) break;
         if (done && s.rnorm <= target) {
-            // relaxed applies: the restart computes the true residual and decides
-            if (used_relaxed) continue;
+            // relaxed applies: accept when the bound on the gap between the
+            // estimate and the true residual, sum_j |y_j| eps ||A z_j|| with
+            // eps = 1e-4 (100x the FP32 apply's measured relative error),
+            // keeps the sum within the target; otherwise the restart computes
+            // the true residual and decides
+            if (used_relaxed) {
+                double gap = 0.0;
+                for (int i = 0; i < k; ++i) gap += std::abs(y[i]) * kRelaxEps * wn[i];
+                if (s.rnorm + gap > target) continue;
+                s.rnorm += gap;
+            }
             s.reason = 2;
             break;
         }

@@ -48,8 +48,12 @@ struct FGMRES {
     int aprec = TDZ_FP64;   // operator apply arithmetic: TDZ_FP64 or TDZ_FP64_DF (FP64 vectors either way)
     // Relaxed Arnoldi applies (inexact Krylov): A z_j in FP32 while the
     // residual r0 = b - A x of every restart stays in aprec. A cycle that
-    // reports convergence is followed by one more restart, whose aprec
-    // residual decides; the result is therefore judged on the true residual.
+    // reports convergence is accepted when the estimate plus the a-posteriori
+    // bound sum_j |y_j| 1e-4 ||A z_j|| on its distance from the true residual
+    // meets the target (the FP32 errors enter scaled by the small y_j once the
+    // start residual is small); otherwise one more restart, whose aprec
+    // residual decides. A relaxed cycle that fails to cut the true residual
+    // tenfold switches the solve back to exact applies.
     bool relaxed = false;
     DevBuf z32, w32;
     long long relaxed_applies = 0;
