@@ -88,11 +88,13 @@ class Clocks:
 
 
 def dist_init():
+    """Replicas: one process per GPU (torchrun env), NCCL on GPUs, gloo without."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world
 
 
@@ -107,7 +109,8 @@ def allmax(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

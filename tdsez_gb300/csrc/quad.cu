@@ -4,7 +4,7 @@
 // multiply by w V with V from the closed form, project back axis by axis and
 // add coef * result to y with atomics (neighbouring elements share
 // coefficients). Work per element 2 d Q (p+1)^d (d-dimensional sum
-// factorisation), the F_TC figure of the survey for this term.
+// factorisation): the per-element tensor-contraction flops of this term.
 #include "quad.h"
 
 #include <cmath>
