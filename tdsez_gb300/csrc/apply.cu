@@ -3,6 +3,8 @@
 #include "apply_kernels.cuh"
 
 #include <atomic>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <type_traits>
@@ -16,6 +18,23 @@ std::map<TuneKey, std::pair<int, int>> g_tune;
 }  // namespace
 
 bool autotune_enabled() { return g_autotune.load() != 0; }
+bool forced_shape(int *txw, int *run) {
+    static const char *v = std::getenv("TDZ_APPLY3D_SHAPE");
+    if (!v) return false;
+    int a = 0, b = 0;
+    if (std::sscanf(v, "%d,%d", &a, &b) != 2 || a <= 0 || b <= 0) return false;
+    *txw = a;
+    *run = b;
+    return true;
+}
+bool smem_attr_exact() {
+    static const bool v = std::getenv("TDZ_APPLY3D_SMEM_EXACT") != nullptr;
+    return v;
+}
+bool tune_verbose() {
+    static const bool v = std::getenv("TDZ_AUTOTUNE_VERBOSE") != nullptr;
+    return v;
+}
 void set_autotune(int on) { g_autotune.store(on ? 1 : 0); }
 bool tune_lookup(const TuneKey &k, int *txw, int *zchunk) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -107,19 +126,25 @@ void launch_1d(const ApplyParams<T> &prm, cudaStream_t st) {
 
 }  // namespace
 
-void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st) {
+void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st,
+                  const void *sub) {
     const int dim = op.sp->dim;
+    auto params = [&](auto tag) {
+        auto prm = make_params<decltype(tag)>(op, pl, x, y);
+        prm.sub = sub;
+        return prm;
+    };
     if (dim == 1) {
         // 1D operators are tiny: the double-float request runs in native FP64
-        if (prec != TDZ_FP32) launch_1d(make_params<double>(op, pl, x, y), st);
-        else launch_1d(make_params<float>(op, pl, x, y), st);
+        if (prec != TDZ_FP32) launch_1d(params(double{}), st);
+        else launch_1d(params(float{}), st);
     } else {
         ApplyParams<float> pf{};
         ApplyParams<double> pd{};
         ApplyParams<dff> pdf{};
-        if (prec == TDZ_FP64) pd = make_params<double>(op, pl, x, y);
-        else if (prec == TDZ_FP64_DF) pdf = make_params<dff>(op, pl, x, y);
-        else pf = make_params<float>(op, pl, x, y);
+        if (prec == TDZ_FP64) pd = params(double{});
+        else if (prec == TDZ_FP64_DF) pdf = params(dff{});
+        else pf = params(float{});
         switch (op.P) {
         case 2: apply_p2(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;
         case 3: apply_p3(dim, pl.hasB, pl.hasC, pf, pd, pdf, prec, st); break;

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstdio>
 #include <type_traits>
 #include <vector>
 
@@ -46,7 +48,19 @@ template <class T> struct ApplyParams {
     T wall_re[2], wall_im[2];   // 1D walls: diagonal values, wall = 0 / n-1
     int walls;
     int za_kind, zc_kind;       // outer combinations: 0 complex, 1 real, 2 imaginary (fewer products)
+    const void *sub;            // non-null: y = sub - op x (a residual), same layout as y
 };
+
+// the value stored at output element e: op x, or sub[e] - op x
+template <class T, class MC, class C>
+__device__ __forceinline__ MC out_value(const ApplyParams<T> &prm, size_t e, C v) {
+    if (prm.sub) {
+        C r = load_c<C>(static_cast<const MC *>(prm.sub)[e]);
+        rfma(r, T(-1.f), v);
+        v = cnorm(r);
+    }
+    return store_c<MC>(v);
+}
 
 // entry o of row i of a combination of base bands
 template <class T, class C>
@@ -61,20 +75,23 @@ __device__ __forceinline__ C comb_at(const CombP<T> &cb, const T *bands, int n, 
 }
 
 // ---------------------------------------------------------------- 3D kernel
-// Per z plane: (1) the prefetched input tile goes to shared memory, (2) barrier,
-// (3) the next plane's tile is requested into registers (its latency overlaps
-// the compute), (4) x stage into sU[buf], (5) barrier, (6) y stage and the
-// outer-stage ring update from sU[buf] and the precomputed band rows. sU is
-// double-buffered, so two barriers per plane suffice.
+// Per z plane, one barrier: the x stage of the next plane and the y and
+// outer stages of this plane, then the prefetched tile after next goes from
+// registers to shared memory and the one after that is requested (its
+// latency overlaps a whole plane of compute). The halo tile and the x-stage
+// results are double-buffered.
 constexpr int kLoadsPerThread3 = 4;   // covers (TY+2p)(TX+2p) / (TX TY) for p <= 5
+
+// ring of output planes: unrolled with fixed slots (FP32) or shifted per plane
+template <class T> constexpr bool kShiftRing = !std::is_same<T, float>::value;
 
 // TX is the largest tile width; the launch may use a narrower one
 // (blockDim.x = 16..TX) to fit n0 with less padding. KA / KC: the kind of the
 // outer combinations fixed at compile time (0 complex, 1 real, 2 imaginary);
 // the double-float CN stage (KC = 2) and mass (KA = 1) get their own
 // instantiations, which save a quarter of the outer-stage products.
-template <class T, int P, bool HB, bool HC, int TX, int TY, int KA = 0, int KC = 0>
-__global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
+template <class T, int P, bool HB, bool HC, int TX, int TY, int KA, int KC>
+__device__ __noinline__ void apply3d_run(const ApplyParams<T> &prm, int x0, int y0, int z0, int z1) {
     using C = typename CT<T>::type;
     constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
     constexpr int NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
@@ -86,25 +103,20 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
     __shared__ T sYs[HC ? BW : 1][TY];
     __shared__ C sYt[HB ? BW : 1][TY];
     extern __shared__ unsigned char dyn_raw[];
-    // dynamic: the halo tile, the double-buffered x-stage results, then the
-    // precomputed outer-band rows of the chunk: [plane][o] (A, C complex; M real)
-    C (*sIn)[RX] = reinterpret_cast<C (*)[RX]>(dyn_raw);
-    C (*sU)[NU][RY][TX] = reinterpret_cast<C (*)[NU][RY][TX]>(dyn_raw + sizeof(C) * RY * RX);
-    C *sZA = reinterpret_cast<C *>(dyn_raw + sizeof(C) * (RY * RX + 2 * NU * RY * TX));
+    // dynamic: the double-buffered halo tile and x-stage results, then the
+    // precomputed outer-band rows of the run: [plane][o] (A, C complex; M real)
+    C (*sIn)[RY][RX] = reinterpret_cast<C (*)[RY][RX]>(dyn_raw);
+    C (*sU)[NU][RY][TX] = reinterpret_cast<C (*)[NU][RY][TX]>(dyn_raw + sizeof(C) * 2 * RY * RX);
+    C *sZA = reinterpret_cast<C *>(dyn_raw + sizeof(C) * (2 * RY * RX + 2 * NU * RY * TX));
     C *sZC = sZA + (size_t)prm.zchunk_planes * BW;
     T *sZM = reinterpret_cast<T *>(sZC + (HC ? (size_t)prm.zchunk_planes * BW : 0));
 
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * txw + tx;
     const int n0 = prm.n0, n1 = prm.n1, n2 = prm.n2;
-    const int tilesX = (n0 + txw - 1) / txw;
-    const int x0 = (blockIdx.x % tilesX) * txw, y0 = (blockIdx.x / tilesX) * TY;
-    const int gx = x0 + tx, gy = y0 + ty;
-    const int z0 = blockIdx.y * prm.zchunk;
-    const int z1 = min(n2, z0 + prm.zchunk);
-    if (z0 >= z1) return;
     using MC = typename MemC<T>::type;
     const MC *__restrict__ X = static_cast<const MC *>(prm.x);
     MC *__restrict__ Y = static_cast<MC *>(prm.y);
+    const int gx = x0 + tx, gy = y0 + ty;
     const int zs = z0 - P;
     const int nplanes = (z1 - z0) + 2 * P;
 
@@ -157,83 +169,155 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const ApplyParams<T> prm) {
         for (int q = 0; q < kLoadsPerThread3; ++q)
             pre[q] = off[q] >= 0 ? load_c<C>(X[(size_t)zin * plane + off[q]]) : czero<C>();
     };
-    const int zfirst = max(zs, 0);
-    load_plane(zfirst);
-
+    // input planes it = lo .. hi-1 (zin = zs + it) lie inside the grid
+    const int lo = max(0, -zs), hi = min(nplanes, n2 - zs);
+    auto store_in = [&](int it) {
+#pragma unroll
+        for (int q = 0; q < kLoadsPerThread3; ++q)
+            if (so[q] >= 0) (&sIn[it & 1][0][0])[so[q]] = pre[q];
+    };
+    auto fetch = [&](int it) {   // plane it into the prefetch registers, if it is in the grid
+        if (it < hi) load_plane(zs + it);
+    };
+    // x stage of plane it: sIn[it & 1] -> sU[it & 1]
+    auto xstage = [&](int it) {
+        const int buf = it & 1;
+        for (int r = ty; r < RY; r += TY) {
+            C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
+#pragma unroll
+            for (int j = 0; j < BW; ++j) {
+                const C v = sIn[buf][r][tx + j];
+                rfma(uM, xm[j], v);
+                if constexpr (HB) cfma(uT, xt[j], v);
+                if constexpr (HC) rfma(uS, xs[j], v);
+            }
+            sU[buf][0][r][tx] = cnorm(uM);
+            if constexpr (HB) sU[buf][UT][r][tx] = cnorm(uT);
+            if constexpr (HC) sU[buf][US][r][tx] = cnorm(uS);
+        }
+    };
+    // y and outer stages of plane it from sU[it & 1]; output plane
+    // zs + it - P + o accumulates in acc[(ring + o) % BW]
     C acc[BW];
 #pragma unroll
     for (int s = 0; s < BW; ++s) acc[s] = czero<C>();
-
-    for (int base = 0; base < nplanes; base += BW) {
+    auto yzstage = [&](int it, int ring) {
+        const int buf = it & 1;
+        C wA = czero<C>(), wB = czero<C>(), wC = czero<C>();
 #pragma unroll
-        for (int ph = 0; ph < BW; ++ph) {
-            const int it = base + ph;
-            if (it >= nplanes) break;
-            const int zin = zs + it;
-            if (zin >= 0 && zin < n2) {
-                const int buf = it & 1;
-#pragma unroll
-                for (int q = 0; q < kLoadsPerThread3; ++q)
-                    if (so[q] >= 0) (&sIn[0][0])[so[q]] = pre[q];
-                __syncthreads();
-                if (zin + 1 < n2 && zin + 1 < z1 + P) load_plane(zin + 1);
-                // x stage
-                for (int r = ty; r < RY; r += TY) {
-                    C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
-#pragma unroll
-                    for (int j = 0; j < BW; ++j) {
-                        const C v = sIn[r][tx + j];
-                        rfma(uM, xm[j], v);
-                        if constexpr (HB) cfma(uT, xt[j], v);
-                        if constexpr (HC) rfma(uS, xs[j], v);
-                    }
-                    sU[buf][0][r][tx] = cnorm(uM);
-                    if constexpr (HB) sU[buf][UT][r][tx] = cnorm(uT);
-                    if constexpr (HC) sU[buf][US][r][tx] = cnorm(uS);
-                }
-                __syncthreads();
-                // y stage
-                C wA = czero<C>(), wB = czero<C>(), wC = czero<C>();
-#pragma unroll
-                for (int j = 0; j < BW; ++j) {
-                    const T ym = sYm[j][ty];
-                    const C um = sU[buf][0][ty + j][tx];
-                    rfma(wA, ym, um);
-                    if constexpr (HB) {
-                        rfma(wB, ym, sU[buf][UT][ty + j][tx]);
-                        cfma(wB, sYt[j][ty], um);
-                    }
-                    if constexpr (HC) {
-                        rfma(wC, ym, sU[buf][US][ty + j][tx]);
-                        rfma(wC, sYs[j][ty], um);
-                    }
-                }
-                wA = cnorm(wA);
-                if constexpr (HB) wB = cnorm(wB);
-                if constexpr (HC) wC = cnorm(wC);
-                // outer (z) stage
-                const C *zA = sZA + (size_t)it * BW;
-#pragma unroll
-                for (int o = 0; o < BW; ++o) {
-                    C &a = acc[(ph - P + o + 2 * BW) % BW];
-                    if constexpr (KA == 1) rfma(a, zA[o].x, wA);
-                    else if constexpr (KA == 2) ifma(a, zA[o].y, wA);
-                    else cfma(a, zA[o], wA);
-                    if constexpr (HB) rfma(a, sZM[(size_t)it * BW + o], wB);
-                    if constexpr (HC) {
-                        const C zc = sZC[(size_t)it * BW + o];
-                        if constexpr (KC == 1) rfma(a, zc.x, wC);
-                        else if constexpr (KC == 2) ifma(a, zc.y, wC);
-                        else cfma(a, zc, wC);
-                    }
-                }
+        for (int j = 0; j < BW; ++j) {
+            const T ym = sYm[j][ty];
+            const C um = sU[buf][0][ty + j][tx];
+            rfma(wA, ym, um);
+            if constexpr (HB) {
+                rfma(wB, ym, sU[buf][UT][ty + j][tx]);
+                cfma(wB, sYt[j][ty], um);
             }
-            if (it >= 2 * P) {
-                const int m = zin - P;
-                if (gx < n0 && gy < n1) Y[((size_t)m * n1 + gy) * n0 + gx] = store_c<MC>(acc[(ph - P + 2 * BW) % BW]);
+            if constexpr (HC) {
+                rfma(wC, ym, sU[buf][US][ty + j][tx]);
+                rfma(wC, sYs[j][ty], um);
             }
-            acc[(ph - P + 2 * BW) % BW] = czero<C>();
         }
+        wA = cnorm(wA);
+        if constexpr (HB) wB = cnorm(wB);
+        if constexpr (HC) wC = cnorm(wC);
+        const C *zA = sZA + (size_t)it * BW;
+#pragma unroll
+        for (int o = 0; o < BW; ++o) {
+            C &a = acc[(ring + o) % BW];
+            if constexpr (KA == 1) rfma(a, zA[o].x, wA);
+            else if constexpr (KA == 2) ifma(a, zA[o].y, wA);
+            else cfma(a, zA[o], wA);
+            if constexpr (HB) rfma(a, sZM[(size_t)it * BW + o], wB);
+            if constexpr (HC) {
+                const C zc = sZC[(size_t)it * BW + o];
+                if constexpr (KC == 1) rfma(a, zc.x, wC);
+                else if constexpr (KC == 2) ifma(a, zc.y, wC);
+                else cfma(a, zc, wC);
+            }
+        }
+    };
+    // Software pipeline, one barrier per plane. Step it (lo <= it < hi): the
+    // x stage of plane it+1 and the y / outer stages of plane it (independent
+    // work between two barriers), then plane it+2 from the registers into
+    // sIn and the request of plane it+3. sIn and sU are double-buffered: the
+    // buffer a step writes was last read before the previous barrier.
+    auto step = [&](int it, int ring) {
+        xstage(it + 1);                // a plane past hi leaves results that nobody reads
+        yzstage(it, ring);
+        store_in(it + 2);
+        fetch(it + 3);
+        __syncthreads();
+    };
+    if (lo < hi) {
+        fetch(lo);
+        store_in(lo);
+        fetch(lo + 1);
+        __syncthreads();
+        xstage(lo);
+        store_in(lo + 1);
+        fetch(lo + 2);
+        __syncthreads();
+    }
+    auto finish = [&](int it, C &out) {   // output plane zs + it - P is complete
+        if (it >= 2 * P) {
+            const int m = zs + it - P;
+            if (gx < n0 && gy < n1) {
+                const size_t e = ((size_t)m * n1 + gy) * n0 + gx;
+                Y[e] = out_value<T, MC>(prm, e, out);
+            }
+        }
+    };
+
+    if constexpr (kShiftRing<T>) {
+        // FP64 / double-float: one copy of the step; the ring shifts down by one
+        // slot per plane (a few register moves), which keeps the long
+        // emulated-FP64 body inside the instruction cache
+#pragma unroll 1
+        for (int it = 0; it < nplanes; ++it) {
+            if (it >= lo && it < hi) step(it, 0);
+            finish(it, acc[0]);
+#pragma unroll
+            for (int s = 0; s + 1 < BW; ++s) acc[s] = acc[s + 1];
+            acc[BW - 1] = czero<C>();
+        }
+    } else {
+        // FP32: the plane loop unrolled by the ring length, fixed slots
+        for (int base = 0; base < nplanes; base += BW) {
+#pragma unroll
+            for (int ph = 0; ph < BW; ++ph) {
+                const int it = base + ph;
+                if (it >= nplanes) break;
+                const int ring = (ph - P + 2 * BW) % BW;
+                if (it >= lo && it < hi) step(it, ring);
+                finish(it, acc[ring]);
+                acc[ring] = czero<C>();
+            }
+        }
+    }
+}
+
+// This CTA owns planes [b L, (b + 1) L) of the (tile, z) order, z fastest
+// (L = prm.zchunk): one or more runs of consecutive planes of one tile, each
+// with its own 2p halo planes. An even split over a grid of about one wave
+// keeps the halo small and leaves no tail wave. A run is a separate
+// (not inlined) function, so the register allocation of its plane loop does
+// not carry the run loop's state.
+template <class T, int P, bool HB, bool HC, int TX, int TY, int KA = 0, int KC = 0>
+__global__ void __launch_bounds__(TX *TY) k_apply3d(const __grid_constant__ ApplyParams<T> prm) {
+    const int txw = blockDim.x;
+    const int n0 = prm.n0, n1 = prm.n1, n2 = prm.n2;
+    const int tilesX = (n0 + txw - 1) / txw;
+    const long long total = (long long)tilesX * ((n1 + TY - 1) / TY) * n2;
+    long long pos = (long long)blockIdx.x * prm.zchunk;
+    const long long end = min(total, pos + prm.zchunk);
+    for (bool first = true; pos < end; first = false) {
+        const int tile = (int)(pos / n2);
+        const int z0 = (int)(pos - (long long)tile * n2);
+        const int z1 = (int)min((long long)n2, z0 + (end - pos));
+        pos += z1 - z0;
+        if (!first) __syncthreads();   // the last run's readers of the band rows are done
+        apply3d_run<T, P, HB, HC, TX, TY, KA, KC>(prm, (tile % tilesX) * txw, (tile / tilesX) * TY, z0, z1);
     }
 }
 
@@ -308,7 +392,7 @@ __global__ void __launch_bounds__(TX) k_apply2d(const ApplyParams<T> prm) {
             }
             if (it >= 2 * P) {
                 const int m = zin - P;
-                if (gx < n0) Y[(size_t)m * n0 + gx] = store_c<MC>(acc[(ph - P + 2 * BW) % BW]);
+                if (gx < n0) Y[(size_t)m * n0 + gx] = out_value<T, MC>(prm, (size_t)m * n0 + gx, acc[(ph - P + 2 * BW) % BW]);
             }
             acc[(ph - P + 2 * BW) % BW] = czero<C>();
         }
@@ -340,6 +424,11 @@ __global__ void k_apply1d(const ApplyParams<T> prm) {
             cfma(acc, comb_at<T, C>(prm.zA, prm.b0, n, bw, i, o), X[j]);
         }
     }
+    if (prm.sub) {
+        const C b = static_cast<const C *>(prm.sub)[i];
+        acc.x = b.x - acc.x;
+        acc.y = b.y - acc.y;
+    }
     Y[i] = acc;
 }
 
@@ -358,21 +447,6 @@ inline int pick_chunk(int tiles, int n_outer, int P, int target = 152 * 8) {
     int chunks = (target + tiles - 1) / tiles;
     chunks = std::max(1, std::min(chunks, n_outer / std::max(1, 4 * P)));
     return (n_outer + chunks - 1) / chunks;
-}
-
-// compute-bound kernels: the chunk count that minimises waves x (chunk + 2p),
-// i.e. the time of the slowest SM including the halo planes each chunk
-// recomputes, for `slots` resident CTAs on the GPU
-inline int pick_chunk_waves(int tiles, int n_outer, int P, int slots) {
-    int best = n_outer;
-    double best_t = 1e300;
-    for (int c = 1; c <= std::max(1, n_outer / std::max(1, 4 * P)); ++c) {
-        const int len = (n_outer + c - 1) / c;
-        const long long ctas = (long long)tiles * ((n_outer + len - 1) / len);
-        const double t = (double)((ctas + slots - 1) / slots) * (len + 2 * P);
-        if (t < best_t - 1e-9) { best_t = t; best = len; }
-    }
-    return best;
 }
 
 // tile width 16..32 (multiple of 4) with the least padding of n0; ties go to the wider
@@ -402,6 +476,12 @@ struct TuneKey {
     }
 };
 bool autotune_enabled();
+bool tune_verbose();   // TDZ_AUTOTUNE_VERBOSE set: the autotuner prints each candidate's time
+// TDZ_APPLY3D_SHAPE="tile_x,run": a fixed launch shape for every 3D apply (no autotuning)
+bool forced_shape(int *txw, int *run);
+// TDZ_APPLY3D_SMEM_EXACT set: raise the dynamic shared-memory limit of a 3D
+// apply kernel only as far as its launches need (default: one opt-in to 200 KB)
+bool smem_attr_exact();
 bool tune_lookup(const TuneKey &k, int *txw, int *zchunk);
 void tune_store(const TuneKey &k, int txw, int zchunk);
 
@@ -411,43 +491,71 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     constexpr int TY = TileY<T, HB, HC>::v, NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
     auto kern = k_apply3d<T, P, HB, HC, kTX3, TY, KA, KC>;
     const bool fp32 = std::is_same<T, float>::value;
-    const size_t tile_smem = sizeof(C) * ((size_t)(TY + 2 * P) * (kTX3 + 2 * P) + 2 * NU * (TY + 2 * P) * kTX3);
+    const size_t tile_smem = sizeof(C) * ((size_t)2 * (TY + 2 * P) * (kTX3 + 2 * P) + 2 * NU * (TY + 2 * P) * kTX3);
     auto smem_for = [&](int zchunk) {
         const size_t rows = (size_t)(zchunk + 2 * P) * (2 * P + 1);
         return tile_smem + rows * sizeof(C) * (HC ? 2 : 1) + (HB ? rows * sizeof(T) : 0);
     };
-    // one opt-in for the largest chunk, then occupancy at that size
-    static int slots = 0;
-    if (!slots) {
-        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(96)));
-        int per_sm = 0, dev = 0, nsm = 0;
-        TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTX3 * TY, smem_for(96)));
+    // shared memory grows with the run length (its band rows, at most n2 + 2p
+    // planes): one opt-in to the largest size, occupancy at the largest size
+    constexpr size_t kMaxDyn = 200 * 1024;
+    static int nsm = 0;
+    if (!nsm) {
+        if (!smem_attr_exact())
+            TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDyn));
+        int dev = 0;
         TDZ_CUDA(cudaGetDevice(&dev));
         TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        slots = std::max(1, per_sm) * nsm;
     }
-    auto tiles_for = [&](int txw) { return ((prm0.n0 + txw - 1) / txw) * ((prm0.n1 + TY - 1) / TY); };
-    auto launch = [&](int txw, int zchunk) {
-        ApplyParams<T> prm = prm0;
-        prm.zchunk = zchunk;
-        prm.zchunk_planes = zchunk + 2 * P;
-        dim3 grid(tiles_for(txw), (prm.n2 + zchunk - 1) / zchunk);
-        kern<<<grid, dim3(txw, TY), smem_for(zchunk), st>>>(prm);
+    const int n2 = prm0.n2;
+    TDZ_CHECK(smem_for(n2) <= kMaxDyn, TDZ_ERR_UNSUPPORTED, "outer axis too long for the 3D apply");
+    static std::atomic<size_t> attr_set{0};
+    auto ensure_smem = [&](size_t need) {
+        if (!smem_attr_exact()) return;
+        size_t cur = attr_set.load();
+        if (need <= cur) return;
+        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        attr_set.store(need);
     };
-    // heuristic: FP32 (HBM-leaning) full warps along x and about 8 CTAs per SM;
-    // FP64 and double-float the least x padding and the fewest waves x (chunk + halo)
+    thread_local int occ_n2 = -1, occ_slots = 0;   // resident CTAs at the last n2 seen
+    if (occ_n2 != n2) {
+        int per_sm = 0;
+        TDZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTX3 * TY, smem_for(n2)));
+        occ_slots = std::max(1, per_sm) * nsm;
+        occ_n2 = n2;
+    }
+    const int slots = occ_slots;
+    auto tiles_for = [&](int txw) { return ((prm0.n0 + txw - 1) / txw) * ((prm0.n1 + TY - 1) / TY); };
+    // run length L for a grid of about g CTAs (no shorter than 4p planes)
+    auto seg_for = [&](int txw, long long g) {
+        const long long total = (long long)tiles_for(txw) * n2;
+        return (int)std::min<long long>(total, std::max<long long>(4 * P, (total + g - 1) / g));
+    };
+    auto launch = [&](int txw, int seg) {
+        ApplyParams<T> prm = prm0;
+        prm.zchunk = seg;
+        prm.zchunk_planes = std::min(seg, n2) + 2 * P;
+        const long long total = (long long)tiles_for(txw) * n2;
+        const unsigned grid = (unsigned)((total + seg - 1) / seg);
+        ensure_smem(smem_for(std::min(seg, n2)));
+        kern<<<grid, dim3(txw, TY), smem_for(std::min(seg, n2)), st>>>(prm);
+    };
+    // heuristic: one wave of persistent CTAs; FP32 full warps along x and two
+    // waves, FP64 and double-float the least x padding
     int txw = fp32 ? kTX3 : pick_tile_x(prm0.n0);
-    int zchunk = fp32 ? std::min(pick_chunk(tiles_for(txw), prm0.n2, P), 96)
-                      : std::min(pick_chunk_waves(tiles_for(txw), prm0.n2, P, slots), 96);
+    int zchunk = seg_for(txw, (long long)slots * (fp32 ? 2 : 1));
     const TuneKey key{reinterpret_cast<const void *>(kern), prm0.n0, prm0.n1, prm0.n2};
-    if (autotune_enabled() && !tune_lookup(key, &txw, &zchunk)) {
+    if (forced_shape(&txw, &zchunk)) {
+        txw = std::max(16, std::min(kTX3, txw / 4 * 4));
+        zchunk = std::max(4 * P, zchunk);
+    } else if (autotune_enabled() && !tune_lookup(key, &txw, &zchunk)) {
         std::vector<std::pair<int, int>> cand;
         for (int t = kTX3; t >= 16; t -= 4) {
             if ((prm0.n0 + t - 1) / t * t > (prm0.n0 + kTX3 - 1) / kTX3 * kTX3) continue;   // more padding than 32
-            const int tl = tiles_for(t);
-            for (int z : {std::min(pick_chunk(tl, prm0.n2, P), 96), std::min(pick_chunk_waves(tl, prm0.n2, P, slots), 96),
-                          std::min(pick_chunk_waves(tl, prm0.n2, P, 2 * slots), 96)})
+            for (int w : {1, 2, 3, 4, 8}) {
+                const int z = seg_for(t, (long long)slots * w);
                 if (std::find(cand.begin(), cand.end(), std::make_pair(t, z)) == cand.end()) cand.push_back({t, z});
+            }
         }
         cudaEvent_t e0, e1;
         TDZ_CUDA(cudaEventCreate(&e0));
@@ -462,6 +570,11 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
             TDZ_CUDA(cudaEventSynchronize(e1));
             float ms = 0.f;
             TDZ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (tune_verbose())
+                std::fprintf(stderr, "tdz autotune apply3d<%s,p%d,B%d,C%d,%d%d> %dx%dx%d: tile %dx%d run %d grid %lld: %.1f us\n",
+                             sizeof(T) == 4 ? "f32" : (std::is_same<T, double>::value ? "f64" : "df"), P, (int)HB,
+                             (int)HC, KA, KC, prm0.n0, prm0.n1, n2, c.first, TY, c.second,
+                             ((long long)tiles_for(c.first) * n2 + c.second - 1) / c.second, 500.f * ms);
             if (ms < best) { best = ms; txw = c.first; zchunk = c.second; }
         }
         TDZ_CUDA(cudaEventDestroy(e0));

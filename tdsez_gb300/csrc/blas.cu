@@ -204,11 +204,11 @@ inline cdff cdf_host(cd a) { return mk_df(dff_from(a.real()), dff_from(a.imag())
 
 // Fused Gram-Schmidt pass on an Arnoldi vector: w += sum_i a_i V_i (the
 // result kept to 48 bits, the precision of the basis), then in the same pass
-// either the dots conj(V_i) w (NORM = false, partial slots 0..K-1) or |w|^2
-// (NORM = true, slot 0): one read of V and w instead of two.
-template <int K, bool NORM>
+// the dots conj(V_i) w (MODE 0: partial slots 0..K-1), |w|^2 (MODE 1: slot 0)
+// or both (MODE 2: slots 0..K-1 and K): one read of V and w instead of two.
+template <int K, int MODE>
 __global__ void __launch_bounds__(kThreads) k_gs_df(double2 *w, PtrPack V, CoefDF a, size_t n, double2 *partial) {
-    constexpr int R = NORM ? 1 : K;
+    constexpr int R = MODE == 1 ? 1 : (MODE == 2 ? K + 1 : K);
     cdff acc[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) acc[i] = czero<cdff>();
@@ -222,12 +222,11 @@ __global__ void __launch_bounds__(kThreads) k_gs_df(double2 *w, PtrPack V, CoefD
         }
         x = cnorm(x);
         w[e] = st_df(x);
-        if constexpr (NORM) {
-            cfma_conj(acc[0], x, x);
-        } else {
+        if constexpr (MODE != 1) {
 #pragma unroll
             for (int i = 0; i < K; ++i) cfma_conj(acc[i], v[i], x);
         }
+        if constexpr (MODE != 0) cfma_conj(acc[R - 1], x, x);
     }
     __shared__ double2 red[kThreads / 32][R];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -422,9 +421,9 @@ void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
 void Reducer::init() {
     if (blocks) return;
     blocks = kRedBlocks;
-    partial.alloc(sizeof(double2) * kMaxDot * blocks);
-    result.alloc(sizeof(double2) * kMaxDot);
-    TDZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host), sizeof(double2) * kMaxDot));
+    partial.alloc(sizeof(double2) * (kMaxDot + 1) * blocks);
+    result.alloc(sizeof(double2) * (kMaxDot + 1));
+    TDZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host), sizeof(double2) * (kMaxDot + 1)));
 }
 
 Reducer::~Reducer() {
@@ -491,7 +490,7 @@ void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec
 void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, size_t n, cd *dots, double *norm,
                cudaStream_t st) {
     TDZ_CHECK(k >= 1 && k <= kMaxDot, TDZ_ERR_INTERNAL, "fused Gram-Schmidt width");
-    TDZ_CHECK((dots != nullptr) != (norm != nullptr), TDZ_ERR_INTERNAL, "dots or norm");
+    TDZ_CHECK(dots != nullptr || norm != nullptr, TDZ_ERR_INTERNAL, "dots or norm");
     r.init();
     PtrPack pp{};
     CoefPack cp{};
@@ -506,25 +505,26 @@ void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, si
     switch (k) {
 #define TDZ_CASE(K)                                                                                       \
     case K:                                                                                               \
-        if (norm) k_gs_df<K, true><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);                  \
-        else k_gs_df<K, false><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);                      \
+        if (dots && norm) k_gs_df<K, 2><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);             \
+        else if (norm) k_gs_df<K, 1><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);               \
+        else k_gs_df<K, 0><<<r.blocks, kThreads, 0, st>>>(wp, pp, cd_, n, part);                         \
         break;
         TDZ_CASE(1) TDZ_CASE(2) TDZ_CASE(3) TDZ_CASE(4) TDZ_CASE(5) TDZ_CASE(6) TDZ_CASE(7) TDZ_CASE(8)
         TDZ_CASE(9) TDZ_CASE(10) TDZ_CASE(11) TDZ_CASE(12) TDZ_CASE(13) TDZ_CASE(14) TDZ_CASE(15) TDZ_CASE(16)
 #undef TDZ_CASE
     default: break;
     }
-    const int nres = norm ? 1 : k;
+    const int nres = (dots ? k : 0) + (norm ? 1 : 0);
     k_finish<<<nres, kThreads, 0, st>>>(part, r.blocks, r.result.as<double2>());
     TDZ_CUDA(cudaGetLastError());
     count_launch(2);
     TDZ_CUDA(cudaMemcpyAsync(r.host, r.result.ptr, sizeof(double2) * nres, cudaMemcpyDeviceToHost, st));
     TDZ_CUDA(cudaStreamSynchronize(st));
-    if (norm) {
-        const double v = r.host[0].x;
-        *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
-    } else {
+    if (dots)
         for (int i = 0; i < k; ++i) dots[i] = cd(r.host[i].x, r.host[i].y);
+    if (norm) {
+        const double v = r.host[nres - 1].x;
+        *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
     }
 }
 

@@ -26,8 +26,8 @@ void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st);
 
 // Reduction workspace: per-block partial sums and device results.
 struct Reducer {
-    DevBuf partial;   // [kMaxDot][blocks] double2
-    DevBuf result;    // [kMaxDot] double2
+    DevBuf partial;   // [kMaxDot + 1][blocks] double2
+    DevBuf result;    // [kMaxDot + 1] double2
     DevBuf hostbuf;   // pinned host mirror of result
     double2 *host = nullptr;
     int blocks = 0;
@@ -50,7 +50,7 @@ void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec
 // ||x||_2 (synchronises)
 double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st);
 // FP64 Arnoldi vector, fused Gram-Schmidt pass (k <= 16): w += sum_i a_i V_i,
-// then either dots[i] = <V_i, w> or *norm = ||w|| from the same pass
+// then dots[i] = <V_i, w> and / or *norm = ||w|| from the same pass
 void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, size_t n, cd *dots, double *norm,
                cudaStream_t st);
 

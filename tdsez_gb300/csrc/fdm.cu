@@ -240,7 +240,8 @@ struct ZSolveParams {
     float *x;               // in/out: real part of (line (i, j), row k) at x[k ks + j js + i is], imaginary at + cs
     size_t ks;
     int js, is, cs;
-    float2 *U;              // scratch: [k][q][line], q = 0..P
+    float2 *ck;             // scratch: elimination state at the start of each row block, [b][e][line]
+    float2 *zb;             // scratch: the band rows of Bc, then of Cc, [2][n2][bw]
     const float *bands;     // outer base bands [nb][n2][bw]
     const float *lx, *ly;   // inner eigenvalues
     int n0, n1, n2;
@@ -248,131 +249,226 @@ struct ZSolveParams {
 };
 
 // One banded complex LU (no pivoting) + solve per line (i, j), one thread
-// per line, lines contiguous in memory (coalesced across the warp). The
-// recursion along z is latency-bound, so (1) the line matrix bands
-// A_z(s) = Bc + s Cc are evaluated once per CTA into shared memory, (2) the
-// right-hand side rows are prefetched 32 rows ahead into a register ring,
-// and the back substitution prefetches its x and U rows 8 rows ahead, and
-// (3) the U scratch keeps the reciprocal pivot, so each row costs one complex
-// reciprocal. Shared memory: 2 n2 (2P+1) float2 (the two band combinations).
-constexpr int kZDist = 32, kZDistB = 8;
+// per line, lines contiguous in memory (coalesced across the warp).
+//
+// The U factor is not stored. The forward pass runs the elimination and the
+// forward substitution down the line and saves only the elimination state
+// (the last P rows of U with their reciprocal pivots, and the last P entries
+// of L^-1 r) at the start of every block of ZBlk::B rows. The backward pass
+// walks the blocks bottom-up: from the block's saved state it redoes the
+// block's elimination (U rows into shared memory, L^-1 r into registers), then
+// back-substitutes the block and writes the solution in place. Per row that
+// is 8 bytes read and the state in the forward pass, 8 bytes read, 8 written
+// and the state in the backward pass (about 40 bytes for P = 3, against
+// 96 with a stored U), and no stores in the forward pass at all. The block's
+// right-hand side and state are prefetched into registers one block ahead;
+// the forward pass streams its rows kZDist ahead through asynchronous copies
+// into shared memory. The band rows of Bc and Cc are evaluated once per solve
+// (k_zbands) and copied into each CTA's shared memory.
+constexpr int kZDist = 32, kZThreads = 128;
+template <int P> struct ZBlk {
+    static constexpr int B = P <= 3 ? 16 : 8;        // rows per block (divides kZDist)
+    static constexpr int NS = P * (P + 1) + P;       // complex entries of the saved state
+    static_assert(B * (P + 1) >= kZDist, "the U block doubles as the forward pass's row ring");
+};
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int P> size_t zsolve_smem(int n2) {
+    return ((size_t)2 * n2 * (2 * P + 1) + (size_t)ZBlk<P>::B * (P + 1) * kZThreads) * sizeof(float2);
+}
+
+// the band rows of A_z(s) = Bc + s Cc for the current stage: [2][n2][2P+1]
+__global__ void k_zbands(const ZSolveParams prm, int bw) {
+    const int n = prm.n2;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * bw; e += gridDim.x * blockDim.x) {
+        const int k = e / bw, o = e % bw;
+        prm.zb[e] = comb_at<float, float2>(prm.Bc, prm.bands, n, bw, k, o);
+        prm.zb[(size_t)n * bw + e] = comb_at<float, float2>(prm.Cc, prm.bands, n, bw, k, o);
+    }
+}
 
 template <int P>
-__global__ void __launch_bounds__(128) k_zsolve(const ZSolveParams prm) {
-    constexpr int BWd = 2 * P + 1;
-    extern __shared__ float2 zs_bands[];
-    float2 *sB = zs_bands, *sC = zs_bands + (size_t)prm.n2 * BWd;
+__global__ void __launch_bounds__(kZThreads) k_zsolve(const ZSolveParams prm) {
+    constexpr int BWd = 2 * P + 1, B = ZBlk<P>::B, NS = ZBlk<P>::NS;
+    static_assert(kZDist % B == 0, "row blocks must tile the prefetch ring");
+    extern __shared__ float2 zs_smem[];
     const int n = prm.n2;
-    for (int e = threadIdx.x; e < n * BWd; e += blockDim.x) {
-        const int k = e / BWd, o = e % BWd;
-        sB[e] = comb_at<float, float2>(prm.Bc, prm.bands, n, BWd, k, o);
-        sC[e] = comb_at<float, float2>(prm.Cc, prm.bands, n, BWd, k, o);
-    }
+    float2 *sB = zs_smem, *sC = zs_smem + (size_t)n * BWd;          // band rows of Bc and Cc
+    float2 *sU = zs_smem + (size_t)2 * n * BWd;                      // [row of block][q][thread]
+    for (int e = threadIdx.x; e < 2 * n * BWd; e += blockDim.x) sB[e] = prm.zb[e];
     __syncthreads();
     const int nl = prm.n0 * prm.n1;
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nl) return;
     const int i = l % prm.n0, j = l / prm.n0;
     const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
-    const size_t stride = (size_t)nl;
     float *xl = prm.x + (size_t)j * prm.js + (size_t)i * prm.is;
     const size_t ks = prm.ks;
     const int cs = prm.cs;
     auto ldx = [&](int k) { const float *q = xl + (size_t)k * ks; return make_float2(q[0], q[cs]); };
     auto stx = [&](int k, float2 v) { float *q = xl + (size_t)k * ks; q[0] = v.x; q[cs] = v.y; };
-    float2 *U = prm.U + l;
+    float2 *ck = prm.ck + l;
+    const size_t cst = (size_t)nl;
+
     float2 Uw[P][P + 1];     // U rows k-1 .. k-P; [0] holds the reciprocal pivot
-    float2 yw[P];            // transformed rhs k-1 .. k-P
+    float2 yw[P];            // L^-1 r at rows k-1 .. k-P
+    auto reset = [&]() {
 #pragma unroll
-    for (int d = 0; d < P; ++d) {
-        yw[d] = make_float2(0.f, 0.f);
+        for (int d = 0; d < P; ++d) {
+            yw[d] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int q = 0; q <= P; ++q) Uw[d][q] = make_float2(1.f, 0.f);
-    }
-    float2 pf[kZDist];
+            for (int q = 0; q <= P; ++q) Uw[d][q] = make_float2(1.f, 0.f);
+        }
+    };
+    // row k: eliminate columns k-P .. k-1 with the U rows in Uw; shifts the
+    // new U row into Uw[0] and L^-1 r into yw[0]
+    auto eliminate = [&](int k, float2 rhs) {
+        float2 a[BWd];
 #pragma unroll
-    for (int u = 0; u < kZDist; ++u) pf[u] = u < n ? ldx(u) : make_float2(0.f, 0.f);
-    for (int k0 = 0; k0 < n; k0 += kZDist) {
+        for (int o = 0; o < BWd; ++o) {
+            const float2 b = sB[k * BWd + o], c = sC[k * BWd + o];
+            a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
+        }
 #pragma unroll
-        for (int u = 0; u < kZDist; ++u) {
-            const int k = k0 + u;
+        for (int d = P; d >= 1; --d) {
+            if (k - d < 0) continue;
+            const float2 *Ur = Uw[d - 1];   // row k-d: Ur[q] = U(k-d, k-d+q), Ur[0] = 1 / U(k-d, k-d)
+            const float2 f = cmulf(a[P - d], Ur[0]);
+#pragma unroll
+            for (int q = 1; q <= P; ++q) {
+                const float2 t = cmulf(f, Ur[q]);
+                a[P - d + q].x -= t.x;
+                a[P - d + q].y -= t.y;
+            }
+            const float2 t = cmulf(f, yw[d - 1]);
+            rhs.x -= t.x;
+            rhs.y -= t.y;
+        }
+        a[P] = crecf(a[P]);
+#pragma unroll
+        for (int d = P - 1; d > 0; --d) {
+            yw[d] = yw[d - 1];
+#pragma unroll
+            for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
+        }
+#pragma unroll
+        for (int q = 0; q <= P; ++q) Uw[0][q] = a[P + q];
+        yw[0] = rhs;
+    };
+
+    // forward pass: the state at the start of blocks 1 .. nb-1. The rows
+    // stream through a kZDist-deep ring in shared memory (this thread's
+    // column of the U block, free until the backward pass) filled by
+    // asynchronous copies, one commit group per row, so kZDist rows are
+    // always in flight whatever the compiler's schedule.
+    reset();
+    {
+        float *ring = reinterpret_cast<float *>(sU + threadIdx.x);   // slot u: ring[2 u kZThreads + {0, 1}]
+        auto issue = [&](int k, int u) {
             if (k < n) {
-                float2 rhs = pf[u];
-                if (k + kZDist < n) pf[u] = ldx(k + kZDist);
-                float2 a[BWd];
+                const float *q = xl + (size_t)k * ks;
+                cp_async4(ring + (size_t)2 * u * kZThreads, q);
+                cp_async4(ring + (size_t)2 * u * kZThreads + 1, q + cs);
+            }
+            cp_async_commit();
+        };
 #pragma unroll
-                for (int o = 0; o < BWd; ++o) {
-                    const float2 b = sB[k * BWd + o], c = sC[k * BWd + o];
-                    a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
-                }
-                // eliminate columns k-P .. k-1 with U rows k-P .. k-1
+        for (int u = 0; u < kZDist; ++u) issue(u, u);
+        for (int k0 = 0; k0 < n; k0 += kZDist) {
 #pragma unroll
-                for (int d = P; d >= 1; --d) {
-                    if (k - d < 0) continue;
-                    const float2 *Ur = Uw[d - 1];   // row k-d: Ur[q] = U(k-d, k-d+q), Ur[0] = 1 / U(k-d, k-d)
-                    const float2 f = cmulf(a[P - d], Ur[0]);
+            for (int u = 0; u < kZDist; ++u) {
+                const int k = k0 + u;
+                if (k < n) {
+                    if (u % B == 0 && k > 0) {
+                        float2 *c = ck + (size_t)(k / B) * NS * cst;
 #pragma unroll
-                    for (int q = 1; q <= P; ++q) {
-                        const float2 t = cmulf(f, Ur[q]);
-                        a[P - d + q].x -= t.x;
-                        a[P - d + q].y -= t.y;
+                        for (int d = 0; d < P; ++d) {
+#pragma unroll
+                            for (int q = 0; q <= P; ++q) c[(size_t)(d * (P + 1) + q) * cst] = Uw[d][q];
+                            c[(size_t)(P * (P + 1) + d) * cst] = yw[d];
+                        }
                     }
-                    const float2 t = cmulf(f, yw[d - 1]);
-                    rhs.x -= t.x;
-                    rhs.y -= t.y;
+                    cp_async_wait<kZDist - 1>();   // row k has landed
+                    const float2 rhs = *reinterpret_cast<const float2 *>(ring + (size_t)2 * u * kZThreads);
+                    issue(k + kZDist, u);
+                    eliminate(k, rhs);
                 }
-                a[P] = crecf(a[P]);
-#pragma unroll
-                for (int d = P - 1; d > 0; --d) {
-                    yw[d] = yw[d - 1];
-#pragma unroll
-                    for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
-                }
-#pragma unroll
-                for (int q = 0; q <= P; ++q) {
-                    Uw[0][q] = a[P + q];
-                    U[((size_t)k * (P + 1) + q) * stride] = a[P + q];
-                }
-                yw[0] = rhs;
-                stx(k, rhs);
             }
         }
+        cp_async_wait<0>();
     }
-    // back substitution, rows n-1 .. 0, prefetching kZDistB rows ahead
+
+    // backward pass, blocks nb-1 .. 0; a block's rows and saved state are
+    // loaded into registers one block ahead
+    const int nb = (n + B - 1) / B;
+    float2 nr[B], nst[NS];
+    auto fetch = [&](int b) {
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            const int k = b * B + r;
+            nr[r] = k < n ? ldx(k) : make_float2(0.f, 0.f);
+        }
+        if (b > 0) {
+            const float2 *c = ck + (size_t)b * NS * cst;
+#pragma unroll
+            for (int e = 0; e < NS; ++e) nst[e] = c[(size_t)e * cst];
+        }
+    };
     float2 xw[P];
 #pragma unroll
     for (int d = 0; d < P; ++d) xw[d] = make_float2(0.f, 0.f);
-    float2 px[kZDistB], pu[kZDistB][P + 1];
+    float2 *su = sU + threadIdx.x;
+    fetch(nb - 1);
+    for (int b = nb - 1; b >= 0; --b) {
+        float2 rr[B];
 #pragma unroll
-    for (int u = 0; u < kZDistB; ++u) {
-        const int k = n - 1 - u;
-        px[u] = k >= 0 ? ldx(k) : make_float2(0.f, 0.f);
+        for (int r = 0; r < B; ++r) rr[r] = nr[r];
+        if (b > 0) {
 #pragma unroll
-        for (int q = 0; q <= P; ++q) pu[u][q] = k >= 0 ? U[((size_t)k * (P + 1) + q) * stride] : make_float2(0.f, 0.f);
-    }
-    for (int k0 = n - 1; k0 >= 0; k0 -= kZDistB) {
+            for (int d = 0; d < P; ++d) {
 #pragma unroll
-        for (int u = 0; u < kZDistB; ++u) {
-            const int k = k0 - u;
-            if (k >= 0) {
-                float2 v = px[u];
-                float2 ur[P + 1];
+                for (int q = 0; q <= P; ++q) Uw[d][q] = nst[d * (P + 1) + q];
+                yw[d] = nst[P * (P + 1) + d];
+            }
+        } else {
+            reset();
+        }
+        if (b > 0) fetch(b - 1);
+        // redo the block's elimination
+        float2 yb[B];
 #pragma unroll
-                for (int q = 0; q <= P; ++q) ur[q] = pu[u][q];
-                const int kn = k - kZDistB;
-                if (kn >= 0) {
-                    px[u] = ldx(kn);
+        for (int r = 0; r < B; ++r) {
+            const int k = b * B + r;
+            yb[r] = make_float2(0.f, 0.f);
+            if (k < n) {
+                eliminate(k, rr[r]);
+                yb[r] = yw[0];
 #pragma unroll
-                    for (int q = 0; q <= P; ++q) pu[u][q] = U[((size_t)kn * (P + 1) + q) * stride];
-                }
+                for (int q = 0; q <= P; ++q) su[(size_t)(r * (P + 1) + q) * kZThreads] = Uw[0][q];
+            }
+        }
+        // back substitution of the block
+#pragma unroll
+        for (int r = B - 1; r >= 0; --r) {
+            const int k = b * B + r;
+            if (k < n) {
+                float2 v = yb[r];
 #pragma unroll
                 for (int q = 1; q <= P; ++q) {
                     if (k + q >= n) continue;
-                    const float2 t = cmulf(ur[q], xw[q - 1]);
+                    const float2 t = cmulf(su[(size_t)(r * (P + 1) + q) * kZThreads], xw[q - 1]);
                     v.x -= t.x;
                     v.y -= t.y;
                 }
-                v = cmulf(v, ur[0]);
+                v = cmulf(v, su[(size_t)(r * (P + 1)) * kZThreads]);
 #pragma unroll
                 for (int d = P - 1; d > 0; --d) xw[d] = xw[d - 1];
                 xw[0] = v;
@@ -384,11 +480,23 @@ __global__ void __launch_bounds__(128) k_zsolve(const ZSolveParams prm) {
 
 template <int P> void launch_zsolve(const ZSolveParams &zp, cudaStream_t st) {
     const int nl = zp.n0 * zp.n1;
-    const size_t smem = (size_t)2 * zp.n2 * (2 * P + 1) * sizeof(float2);
+    const size_t smem = zsolve_smem<P>(zp.n2);
     TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
     if (smem > 48 * 1024)
         TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_zsolve<P><<<(nl + 127) / 128, 128, smem, st>>>(zp);
+    k_zbands<<<(zp.n2 * (2 * P + 1) + 255) / 256, 256, 0, st>>>(zp, 2 * P + 1);
+    k_zsolve<P><<<(nl + kZThreads - 1) / kZThreads, kZThreads, smem, st>>>(zp);
+}
+
+// saved-state scratch of the line solves (float2 entries)
+size_t zsolve_state_size(int P, int n2, size_t lines) {
+    auto sz = [&](int B, int NS) { return (size_t)((n2 + B - 1) / B) * NS * lines; };
+    switch (P) {
+    case 2: return sz(ZBlk<2>::B, ZBlk<2>::NS);
+    case 3: return sz(ZBlk<3>::B, ZBlk<3>::NS);
+    case 4: return sz(ZBlk<4>::B, ZBlk<4>::NS);
+    default: return sz(ZBlk<5>::B, ZBlk<5>::NS);
+    }
 }
 
 CombP<float> eval_combf(const Comb &c, const std::array<cd, 5> &sg, cd extra_scale = 1.0) {
@@ -443,7 +551,8 @@ void PcFDM::setup(Operator *op_) {
             upload(VT[d], vt32);
         }
     }
-    ufac.alloc(N * (P + 1) * sizeof(float2));
+    ufac.alloc(zsolve_state_size(P, n[dim - 1], N / n[dim - 1]) * sizeof(float2));
+    zb.alloc((size_t)2 * n[dim - 1] * (2 * P + 1) * sizeof(float2));
     if (tensor) {
         ldx = (n[0] + 3) / 4 * 4;
         ldy = (n[1] + 3) / 4 * 4;
@@ -467,7 +576,8 @@ ZSolveParams line_params(const PcFDM &f) {
     const std::array<cd, 5> &sg = op->sigma;
     const int outer = dim - 1;
     ZSolveParams zp{};
-    zp.U = f.ufac.as<float2>();
+    zp.ck = f.ufac.as<float2>();
+    zp.zb = f.zb.as<float2>();
     zp.bands = op->dev32[outer].as<float>();
     zp.lx = f.lam[0].as<float>();
     zp.ly = dim == 3 ? f.lam[1].as<float>() : nullptr;
@@ -500,7 +610,7 @@ void line_solve(int P, const ZSolveParams &zp, cudaStream_t st) {
     case 5: launch_zsolve<5>(zp, st); break;
     }
     TDZ_CUDA(cudaGetLastError());
-    count_launch();
+    count_launch(2);
 }
 
 }  // namespace

@@ -25,8 +25,8 @@ struct PcFDM : Precond {
     size_t N = 0;
     DevBuf V[2], VT[2];        // FP32 n_d x n_d (row-major) eigenvectors and their transpose
     DevBuf lam[2];             // FP32 eigenvalues per inner axis
-    DevBuf zb;                 // FP32 outer base bands (a copy of the operator's)
-    DevBuf b1, b2, ufac;       // FP32 work vectors and the U factors of the line solves
+    DevBuf zb;                 // FP32 band rows of the line matrices, Bc then Cc, [2][n_outer][2P+1]
+    DevBuf b1, b2, ufac;       // FP32 work vectors and the saved elimination states of the line solves
     bool exact = true;         // false: inner one-axis terms other than stiffness were dropped
     // 3D with n_x, n_y <= 256: transforms on the tensor cores (tcgen05, TF32 hi/lo split) over
     // row-planar FP32 buffers pa ([z][y][c][x], pitch ldx) and pb ([z][x][c][y], pitch ldy)

@@ -59,9 +59,8 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     while (true) {
         // r = b - A x  -> V0
         double2 *v0 = V[0].as<double2>();
-        op->apply(TDZ_STAGE, aprec, x, v0, st);
+        op->residual(TDZ_STAGE, aprec, x, b, v0, st);
         ++applies;
-        blas::axpby(v0, 1.0, b, -1.0, n, TDZ_FP64, st);
         const double beta = blas::nrm2(red, v0, n, TDZ_FP64, st);
         if (!std::isfinite(beta)) { s.reason = -9; s.rnorm = beta; break; }
         s.rnorm = beta;
@@ -98,9 +97,39 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h.data(), st);
             for (int i = 0; i <= j; ++i) h[i] = -h[i];
             if (j + 1 <= 16) {
-                blas::gs_update(red, wv, j + 1, Vp.data(), h.data(), n, h2.data(), nullptr, st);
+                double w1 = 0.0;
+                blas::gs_update(red, wv, j + 1, Vp.data(), h.data(), n, h2.data(), &w1, st);
                 for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
-                blas::gs_update(red, wv, j + 1, Vp.data(), h2.data(), n, nullptr, &hn, st);
+                // The second pass only restores the orthogonality of w for the
+                // next basis vector. If the least-squares residual with this
+                // column already meets the target (with a 2x margin), the
+                // iteration ends here: the column is h + h2 and its
+                // subdiagonal ||w - sum h2_i V_i|| = sqrt(||w||^2 - sum |h2_i|^2)
+                // (orthonormal V), so the Arnoldi relation holds as for the
+                // second pass.
+                bool early = false;
+                if (!relax && std::isfinite(w1)) {
+                    double q = w1 * w1;
+                    for (int i = 0; i <= j; ++i) q -= std::norm(h2[i]);
+                    const double hn1 = std::sqrt(std::max(q, 0.0));
+                    // residual after this column: |g_j| hn / sqrt(|c|^2 + hn^2), c the
+                    // diagonal entry after the previous rotations
+                    std::vector<cd> col(j + 1);
+                    for (int i = 0; i <= j; ++i) col[i] = -(h[i] + h2[i]);
+                    for (int i = 0; i < j; ++i) {
+                        const cd a0 = col[i], b0 = col[i + 1];
+                        col[i] = std::conj(cs[i]) * a0 + std::conj(sn[i]) * b0;
+                        col[i + 1] = -sn[i] * a0 + cs[i] * b0;
+                    }
+                    const double rr = std::sqrt(std::norm(col[j]) + hn1 * hn1);
+                    const double est = rr > 0.0 ? std::abs(g[j]) * hn1 / rr : std::abs(g[j]);
+                    if (est <= 0.5 * target) {
+                        early = true;
+                        hn = hn1;
+                        ++early_accepts;
+                    }
+                }
+                if (!early) blas::gs_update(red, wv, j + 1, Vp.data(), h2.data(), n, nullptr, &hn, st);
             } else {
                 blas::maxpy(wv, j + 1, Vp.data(), h.data(), n, TDZ_FP64, st);
                 blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h2.data(), st);

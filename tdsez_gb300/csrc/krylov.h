@@ -45,6 +45,7 @@ struct FGMRES {
     blas::Reducer red;
     SolveStats last;
     long long applies = 0;
+    long long early_accepts = 0;   // iterations that met the target after one Gram-Schmidt pass
     int aprec = TDZ_FP64;   // operator apply arithmetic: TDZ_FP64 or TDZ_FP64_DF (FP64 vectors either way)
     // Relaxed Arnoldi applies (inexact Krylov): A z_j in FP32 while the
     // residual r0 = b - A x of every restart stays in aprec. A cycle that

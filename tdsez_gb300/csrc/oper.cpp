@@ -259,18 +259,20 @@ void Operator::set_stage(cd alpha, cd g, const std::vector<cd> &c) {
     stage_set = true;
 }
 
-void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t st) {
+void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t st) { residual(which, prec, x, nullptr, y, st); }
+
+void Operator::residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st) {
     TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG,
               "precision must be TDZ_FP32, TDZ_FP64 or TDZ_FP64_DF");
     TDZ_CHECK(x && y, TDZ_ERR_ARG, "null vector");
     TDZ_CHECK(x != y, TDZ_ERR_ARG, "x and y must not alias");
     if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");
     Plan &pl = plan(which);
-    launch_apply(*this, pl, prec, x, y, st);
+    launch_apply(*this, pl, prec, x, y, st, b);
     if (quad.on && (which == TDZ_HAMILTONIAN || which == TDZ_STAGE)) {
-        // y += s (g for the stage) V_q x
+        // y += s (g for the stage) V_q x; minus that for a residual
         const cd coef = -phys.charge * (which == TDZ_STAGE ? sigma[1] : cd(1.0));
-        quad.apply(coef, prec, x, y, st);
+        quad.apply(b ? -coef : coef, prec, x, y, st);
     }
     ++launches;
 }

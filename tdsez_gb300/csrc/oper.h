@@ -75,6 +75,8 @@ struct Operator {
     void compile(Plan &pl, const std::vector<Term> &ts) const;
     void set_stage(cd alpha, cd g, const std::vector<cd> &c);
     void apply(int which, int prec, const void *x, void *y, cudaStream_t st);
+    // y = b - op x in one pass (b and y FP64 for TDZ_FP64 / TDZ_FP64_DF)
+    void residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st);
     // <psi|M|psi>, <psi|H|psi>, <psi|D_a|psi> (FP64 psi); see tdz_observables
     std::vector<DevBuf> obs_buf;
     void observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
@@ -87,6 +89,8 @@ enum BaseId { kM = 0, kS = 1, kX = 2 };
 void set_autotune(int on);
 
 // kernel launchers (apply.cu)
-void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st);
+// y = op x, or y = sub - op x when sub is non-null (the residual, fused into the store)
+void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st,
+                  const void *sub = nullptr);
 
 }  // namespace tdz
