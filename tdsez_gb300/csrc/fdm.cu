@@ -478,24 +478,334 @@ __global__ void __launch_bounds__(kZThreads) k_zsolve(const ZSolveParams prm) {
     }
 }
 
+// ---- twisted line solve: two threads per line
+// The line is cut at the twist m (a multiple of the block length). One thread
+// factors rows 0 .. m-1 from the top, its partner rows n-1 .. m from the
+// bottom (the same elimination on the reversed line: for a complex-symmetric
+// band matrix, row k read backwards). Each half's elimination runs over the
+// band's columns past its end too, so its last P rows of U carry the
+// coupling to the other half. The two final elimination states meet in shared
+// memory, where both threads solve the same 2P x 2P system for the P unknowns
+// on either side of the twist: with the tail rows scaled by the reciprocal
+// pivots, U1 T1 + W1 T2 = c1 and U2 T2 + W2 T1 = c2 (U unit upper
+// triangular), so S T2 = c2 - W2 U1^-1 c1 with S = U2 - W2 U1^-1 W1, and
+// T1 = U1^-1 (c1 - W1 T2). Each thread then back-substitutes its half from the
+// partner's tail values. This doubles the threads of the latency-bound
+// recursion and halves its length.
+constexpr int kZ2Lines = 64;                     // lines per CTA (two threads each)
+template <int P> struct ZBlk2 {
+    static constexpr int B = P == 2 ? 16 : 8;    // rows per block
+    static constexpr int NS = P * (P + 1) + P;
+    static_assert(B * (P + 1) >= kZDist, "the U block doubles as the row ring");
+    static_assert(NS <= B * (P + 1), "the U block doubles as the exchange buffer");
+};
+
+template <int P> size_t zsolve2_smem(int n2) {
+    return ((size_t)2 * n2 * (2 * P + 1) + (size_t)ZBlk2<P>::B * (P + 1) * 2 * kZ2Lines) * sizeof(float2);
+}
+__host__ __device__ inline int zsolve2_twist(int n2, int B) { return B * ((n2 + B) / (2 * B)); }
+
+__device__ __forceinline__ float2 csubf(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+template <int P>
+__global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm) {
+    constexpr int BWd = 2 * P + 1, B = ZBlk2<P>::B, NS = ZBlk2<P>::NS, T = 2 * kZ2Lines;
+    static_assert(kZDist % B == 0, "row blocks must tile the prefetch ring");
+    extern __shared__ float2 zs_smem[];
+    const int n = prm.n2;
+    float2 *sB = zs_smem, *sC = zs_smem + (size_t)n * BWd;
+    float2 *sU = zs_smem + (size_t)2 * n * BWd;   // [slot][thread]: row ring, exchange, U block
+    for (int e = threadIdx.x; e < 2 * n * BWd; e += blockDim.x) sB[e] = prm.zb[e];
+    __syncthreads();
+    const int half = threadIdx.x / kZ2Lines;       // 0: rows 0 .. m-1, 1: rows n-1 .. m
+    const int li = threadIdx.x % kZ2Lines;
+    const int nl = prm.n0 * prm.n1;
+    const int lraw = blockIdx.x * kZ2Lines + li;
+    const bool valid = lraw < nl;
+    const int l = valid ? lraw : nl - 1;           // idle threads shadow a real line, store nothing
+    const int m = zsolve2_twist(n, B);
+    const int L = half ? n - m : m;                // rows of this half
+    const int i = l % prm.n0, j = l / prm.n0;
+    const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
+    float *xl = prm.x + (size_t)j * prm.js + (size_t)i * prm.is;
+    const size_t ks = prm.ks;
+    const int cs = prm.cs;
+    auto phys = [&](int k) { return half ? n - 1 - k : k; };
+    auto ldx = [&](int k) { const float *q = xl + (size_t)phys(k) * ks; return make_float2(q[0], q[cs]); };
+    auto stx = [&](int k, float2 v) {
+        if (valid) {
+            float *q = xl + (size_t)phys(k) * ks;
+            q[0] = v.x;
+            q[cs] = v.y;
+        }
+    };
+    const size_t cst = (size_t)nl;
+    float2 *ck = prm.ck + (size_t)(half ? (m + B - 1) / B : 0) * NS * cst + l;
+
+    float2 Uw[P][P + 1];
+    float2 yw[P];
+    auto reset = [&]() {
+#pragma unroll
+        for (int d = 0; d < P; ++d) {
+            yw[d] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q <= P; ++q) Uw[d][q] = make_float2(1.f, 0.f);
+        }
+    };
+    // local row k of this half (its band row read backwards in the bottom half)
+    auto eliminate = [&](int k, float2 rhs) {
+        float2 a[BWd];
+        const int pr = phys(k);
+#pragma unroll
+        for (int o = 0; o < BWd; ++o) {
+            const int oo = half ? 2 * P - o : o;
+            const float2 b = sB[pr * BWd + oo], c = sC[pr * BWd + oo];
+            a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
+        }
+#pragma unroll
+        for (int d = P; d >= 1; --d) {
+            if (k - d < 0) continue;
+            const float2 *Ur = Uw[d - 1];
+            const float2 f = cmulf(a[P - d], Ur[0]);
+#pragma unroll
+            for (int q = 1; q <= P; ++q) {
+                const float2 t = cmulf(f, Ur[q]);
+                a[P - d + q].x -= t.x;
+                a[P - d + q].y -= t.y;
+            }
+            const float2 t = cmulf(f, yw[d - 1]);
+            rhs.x -= t.x;
+            rhs.y -= t.y;
+        }
+        a[P] = crecf(a[P]);
+#pragma unroll
+        for (int d = P - 1; d > 0; --d) {
+            yw[d] = yw[d - 1];
+#pragma unroll
+            for (int q = 0; q <= P; ++q) Uw[d][q] = Uw[d - 1][q];
+        }
+#pragma unroll
+        for (int q = 0; q <= P; ++q) Uw[0][q] = a[P + q];
+        yw[0] = rhs;
+    };
+
+    // forward pass of this half, rows streamed through the ring
+    reset();
+    {
+        float *ring = reinterpret_cast<float *>(sU + threadIdx.x);
+        auto issue = [&](int k, int u) {
+            if (k < L) {
+                const float *q = xl + (size_t)phys(k) * ks;
+                cp_async4(ring + (size_t)2 * u * T, q);
+                cp_async4(ring + (size_t)2 * u * T + 1, q + cs);
+            }
+            cp_async_commit();
+        };
+#pragma unroll
+        for (int u = 0; u < kZDist; ++u) issue(u, u);
+        for (int k0 = 0; k0 < L; k0 += kZDist) {
+#pragma unroll
+            for (int u = 0; u < kZDist; ++u) {
+                const int k = k0 + u;
+                if (k < L) {
+                    if (u % B == 0 && k > 0 && valid) {
+                        float2 *c = ck + (size_t)(k / B) * NS * cst;
+#pragma unroll
+                        for (int d = 0; d < P; ++d) {
+#pragma unroll
+                            for (int q = 0; q <= P; ++q) c[(size_t)(d * (P + 1) + q) * cst] = Uw[d][q];
+                            c[(size_t)(P * (P + 1) + d) * cst] = yw[d];
+                        }
+                    }
+                    cp_async_wait<kZDist - 1>();
+                    const float2 rhs = *reinterpret_cast<const float2 *>(ring + (size_t)2 * u * T);
+                    issue(k + kZDist, u);
+                    eliminate(k, rhs);
+                }
+            }
+        }
+        cp_async_wait<0>();
+    }
+
+    // exchange the final states and solve the twist system (same arithmetic in both threads)
+    float2 *ex = sU;   // [e][thread]
+#pragma unroll
+    for (int d = 0; d < P; ++d) {
+#pragma unroll
+        for (int q = 0; q <= P; ++q) ex[(size_t)(d * (P + 1) + q) * T + threadIdx.x] = Uw[d][q];
+        ex[(size_t)(P * (P + 1) + d) * T + threadIdx.x] = yw[d];
+    }
+    __syncthreads();
+    float2 U1[P][P], W1[P][P], c1[P], U2[P][P], W2[P][P], c2[P];
+    auto tail = [&](int col, float2 (&U)[P][P], float2 (&W)[P][P], float2 (&c)[P]) {
+        auto st = [&](int e) { return ex[(size_t)e * T + col]; };
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            const int d = P - 1 - r;
+            const float2 rp = st(d * (P + 1));
+#pragma unroll
+            for (int k = 0; k < P; ++k) {
+                U[r][k] = k > r ? cmulf(rp, st(d * (P + 1) + (k - r))) : make_float2(0.f, 0.f);
+                W[r][k] = k >= P - 1 - r ? cmulf(rp, st(d * (P + 1) + (2 * P - 1 - r - k))) : make_float2(0.f, 0.f);
+            }
+            c[r] = cmulf(rp, st(P * (P + 1) + d));
+        }
+    };
+    tail(li, U1, W1, c1);
+    tail(li + kZ2Lines, U2, W2, c2);
+    __syncthreads();   // the exchange buffer is this thread's U block from here on
+    // z1 = U1^-1 c1, M1 = U1^-1 W1 (unit upper triangular)
+    float2 z1[P], M1[P][P];
+#pragma unroll
+    for (int r = P - 1; r >= 0; --r) {
+        z1[r] = c1[r];
+#pragma unroll
+        for (int k = 0; k < P; ++k) M1[r][k] = W1[r][k];
+#pragma unroll
+        for (int q = r + 1; q < P; ++q) {
+            z1[r] = csubf(z1[r], cmulf(U1[r][q], z1[q]));
+#pragma unroll
+            for (int k = 0; k < P; ++k) M1[r][k] = csubf(M1[r][k], cmulf(U1[r][q], M1[q][k]));
+        }
+    }
+    // S = U2 + I - W2 M1 (U2 holds the strict upper part), g = c2 - W2 z1
+    float2 S[P][P], g[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+        g[r] = c2[r];
+#pragma unroll
+        for (int k = 0; k < P; ++k) S[r][k] = k == r ? make_float2(1.f, 0.f) : U2[r][k];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            g[r] = csubf(g[r], cmulf(W2[r][q], z1[q]));
+#pragma unroll
+            for (int k = 0; k < P; ++k) S[r][k] = csubf(S[r][k], cmulf(W2[r][q], M1[q][k]));
+        }
+    }
+    // S T2 = g: Gaussian elimination without pivoting, then T1 = z1 - M1 T2
+#pragma unroll
+    for (int c = 0; c < P; ++c) {
+        const float2 inv = crecf(S[c][c]);
+#pragma unroll
+        for (int r = c + 1; r < P; ++r) {
+            const float2 f = cmulf(S[r][c], inv);
+#pragma unroll
+            for (int k = c + 1; k < P; ++k) S[r][k] = csubf(S[r][k], cmulf(f, S[c][k]));
+            g[r] = csubf(g[r], cmulf(f, g[c]));
+        }
+        S[c][c] = inv;
+    }
+    float2 T2[P], T1[P];
+#pragma unroll
+    for (int r = P - 1; r >= 0; --r) {
+        float2 v = g[r];
+#pragma unroll
+        for (int k = r + 1; k < P; ++k) v = csubf(v, cmulf(S[r][k], T2[k]));
+        T2[r] = cmulf(v, S[r][r]);
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+        T1[r] = z1[r];
+#pragma unroll
+        for (int k = 0; k < P; ++k) T1[r] = csubf(T1[r], cmulf(M1[r][k], T2[k]));
+    }
+
+    // backward pass of this half; row L + c of this half is the partner's tail row P-1-c
+    const int nb = (L + B - 1) / B;
+    float2 nr[B], nst[NS];
+    auto fetch = [&](int b) {
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            const int k = b * B + r;
+            nr[r] = k < L ? ldx(k) : make_float2(0.f, 0.f);
+        }
+        if (b > 0) {
+            const float2 *c = ck + (size_t)b * NS * cst;
+#pragma unroll
+            for (int e = 0; e < NS; ++e) nst[e] = c[(size_t)e * cst];
+        }
+    };
+    float2 xw[P];
+#pragma unroll
+    for (int c = 0; c < P; ++c) xw[c] = half ? T1[P - 1 - c] : T2[P - 1 - c];
+    float2 *su = sU + threadIdx.x;
+    fetch(nb - 1);
+    for (int b = nb - 1; b >= 0; --b) {
+        float2 rr[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) rr[r] = nr[r];
+        if (b > 0) {
+#pragma unroll
+            for (int d = 0; d < P; ++d) {
+#pragma unroll
+                for (int q = 0; q <= P; ++q) Uw[d][q] = nst[d * (P + 1) + q];
+                yw[d] = nst[P * (P + 1) + d];
+            }
+        } else {
+            reset();
+        }
+        if (b > 0) fetch(b - 1);
+        float2 yb[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            const int k = b * B + r;
+            yb[r] = make_float2(0.f, 0.f);
+            if (k < L) {
+                eliminate(k, rr[r]);
+                yb[r] = yw[0];
+#pragma unroll
+                for (int q = 0; q <= P; ++q) su[(size_t)(r * (P + 1) + q) * T] = Uw[0][q];
+            }
+        }
+#pragma unroll
+        for (int r = B - 1; r >= 0; --r) {
+            const int k = b * B + r;
+            if (k < L) {
+                float2 v = yb[r];
+#pragma unroll
+                for (int q = 1; q <= P; ++q) v = csubf(v, cmulf(su[(size_t)(r * (P + 1) + q) * T], xw[q - 1]));
+                v = cmulf(v, su[(size_t)(r * (P + 1)) * T]);
+#pragma unroll
+                for (int d = P - 1; d > 0; --d) xw[d] = xw[d - 1];
+                xw[0] = v;
+                stx(k, v);
+            }
+        }
+    }
+}
+
 template <int P> void launch_zsolve(const ZSolveParams &zp, cudaStream_t st) {
     const int nl = zp.n0 * zp.n1;
+    k_zbands<<<(zp.n2 * (2 * P + 1) + 255) / 256, 256, 0, st>>>(zp, 2 * P + 1);
+    if (zp.n2 >= 4 * ZBlk2<P>::B) {
+        const size_t smem = zsolve2_smem<P>(zp.n2);
+        TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
+        if (smem > 48 * 1024)
+            TDZ_CUDA(cudaFuncSetAttribute(k_zsolve2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_zsolve2<P><<<(nl + kZ2Lines - 1) / kZ2Lines, 2 * kZ2Lines, smem, st>>>(zp);
+        return;
+    }
     const size_t smem = zsolve_smem<P>(zp.n2);
     TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
     if (smem > 48 * 1024)
         TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_zbands<<<(zp.n2 * (2 * P + 1) + 255) / 256, 256, 0, st>>>(zp, 2 * P + 1);
     k_zsolve<P><<<(nl + kZThreads - 1) / kZThreads, kZThreads, smem, st>>>(zp);
 }
 
-// saved-state scratch of the line solves (float2 entries)
+// saved-state scratch of the line solves (float2 entries): the larger of the
+// one-thread and the two-thread layouts
 size_t zsolve_state_size(int P, int n2, size_t lines) {
-    auto sz = [&](int B, int NS) { return (size_t)((n2 + B - 1) / B) * NS * lines; };
+    auto sz = [&](int B, int NS, int B2) {
+        const int m = zsolve2_twist(n2, B2);
+        const size_t one = (size_t)((n2 + B - 1) / B) * NS * lines;
+        const size_t two = (size_t)((m + B2 - 1) / B2 + (n2 - m + B2 - 1) / B2) * NS * lines;
+        return std::max(one, two);
+    };
     switch (P) {
-    case 2: return sz(ZBlk<2>::B, ZBlk<2>::NS);
-    case 3: return sz(ZBlk<3>::B, ZBlk<3>::NS);
-    case 4: return sz(ZBlk<4>::B, ZBlk<4>::NS);
-    default: return sz(ZBlk<5>::B, ZBlk<5>::NS);
+    case 2: return sz(ZBlk<2>::B, ZBlk<2>::NS, ZBlk2<2>::B);
+    case 3: return sz(ZBlk<3>::B, ZBlk<3>::NS, ZBlk2<3>::B);
+    case 4: return sz(ZBlk<4>::B, ZBlk<4>::NS, ZBlk2<4>::B);
+    default: return sz(ZBlk<5>::B, ZBlk<5>::NS, ZBlk2<5>::B);
     }
 }
 

@@ -66,6 +66,20 @@ def _c4():
                 coupled=(2,))
 
 
+def heterostructure_lines(p, nel_z):
+    """3D heterostructure with short x / y axes and a long layered z axis: the
+    FDM line solves along z take the two-thread (twisted) path once z has
+    4 blocks of rows (32 rows for p = 3..5, 64 for p = 2)."""
+    nq = p + 1
+    br = [-9.0, 4.0]
+    knots = [ob.uniform_knots(4, -8.0, 8.0, p), ob.uniform_knots(3, -7.0, 7.0, p),
+             ob.interface_knots(-20.0, 20.0, nel_z, p, br)]
+    m = _layered(br, [0.067, 0.092, 0.067])
+    V = [None, None, _layered(br, [0.0, -0.2, 0.1])]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass_axis=2, inv_mass=lambda z: 1.0 / m(z), V=V,
+                coupled=(2,))
+
+
 @case("3d_const_mass_cap")
 def _c5():
     p, nq = 4, 5
