@@ -1,21 +1,23 @@
 // tcgen05 transform kernel (see tgemm.h).
 //
 // Persistent CTAs (one per SM, 160 threads) walk 256 x Np output tiles (two
-// 128-row sub-tiles; 128 x Np when Np > 192), 64 complex rows per sub-tile with
-// real and imaginary part rows interleaved; the accumulators live in tensor
-// memory (TMEM, columns 0 and 256). K runs in chunks of
-// 32 (one 128-byte swizzled row per operand row) through an NS-stage ring
-// (NS = 3, or 2 for Np > 192) that warp 4 fills with TMA
-// (cp.async.bulk.tensor, 128-byte swizzle) up to NS chunks ahead, across tile
-// boundaries:
-//   stage = A (128 x 32 FP32, split by warps 0-3 in place into TF32 hi, with
+// 128-row sub-tiles), 64 complex rows per sub-tile with real and imaginary
+// part rows interleaved; the accumulators live in tensor memory (TMEM,
+// columns 0 and 256). K runs in chunks of 16 (one 64-byte swizzled row per
+// operand row) through an NS-stage ring (as many stages as fit, 5 for
+// Np = 176) that warp 4 fills with TMA (cp.async.bulk.tensor, 64-byte
+// swizzle) up to NS chunks ahead, across tile boundaries:
+//   stage = A (256 x 16 FP32, split by warps 0-3 in place into TF32 hi, with
 //           the lo part in one of two extra buffers; both rounded to nearest)
-//         + B hi, B lo (Np x 32 each, split on the host).
+//         + B hi, B lo (Np x 16 each, split on the host).
+// Short chunks and a deep ring keep several chunks of loads in flight behind
+// the MMAs (with two 32-wide stages the loads of a chunk could only start
+// when the MMAs two chunks back had finished, which left the tensor pipe idle
+// most of the time).
 // Per 8-wide K step thread 0 issues four MMAs,
 //   D += A_hi B_hi + A_hi B_lo + A_lo B_hi + A_lo B_lo,
 // the full product of the hi/lo splits (each part rounded to TF32), so the
-// result has FP32 accuracy at TF32 tensor-core rates (the transform is bound
-// by its loads, not by the tensor pipe). At the end
+// result has FP32 accuracy at TF32 tensor-core rates. At the end
 // of a tile warps 0-3 read TMEM with tcgen05.ld (warp w owns lanes
 // 32w..32w+31, lane = tile row) and store the tile transposed per plane.
 // Every wait on an mbarrier is bounded (clock64): on time-out the kernel sets
@@ -34,8 +36,8 @@ namespace tdz {
 namespace {
 
 constexpr int TM = 128;        // tile rows (GEMM rows)
-constexpr int KC = 32;         // K per stage (128 bytes of FP32)
-constexpr int A_BYTES = TM * KC * 4;   // 16 KB
+constexpr int KC = 16;         // K per stage (64 bytes of FP32: one 64-byte swizzled row)
+constexpr int A_BYTES = TM * KC * 4;   // 8 KB
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
 __device__ int g_tgemm_error = 0;
@@ -85,15 +87,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-// shared-memory matrix descriptor: K-major operand in the canonical 128-byte
-// swizzled layout (8-row groups 1024 bytes apart), start address addr
+// shared-memory matrix descriptor: K-major operand in the canonical 64-byte
+// swizzled layout (8-row groups 512 bytes apart), start address addr
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     uint64_t d = 0;
     d |= (uint64_t)((addr & 0x3FFFF) >> 4);          // start address >> 4      bits  0-13
     d |= (uint64_t)1 << 16;                          // leading offset (unused) bits 16-29
-    d |= (uint64_t)(1024 >> 4) << 32;                // stride offset 1024 B    bits 32-45
+    d |= (uint64_t)((8 * KC * 4) >> 4) << 32;        // stride offset 512 B     bits 32-45
     d |= (uint64_t)1 << 46;                          // descriptor version      bits 46-47
-    d |= (uint64_t)2 << 61;                          // 128-byte swizzle        bits 61-63
+    d |= (uint64_t)4 << 61;                          // 64-byte swizzle         bits 61-63
     return d;
 }
 
@@ -150,12 +152,19 @@ __device__ __forceinline__ void bar_sync(int id, int count) {
 
 // MS = 128-row sub-tiles per tile (1 or 2): with 2, each B chunk loaded by TMA
 // serves 256 rows (two accumulators in TMEM at columns 0 and 256)
+// Stages: as many as fit (up to 6), so that a stage's loads have several
+// chunks of MMA time to land.
 template <int NP, int MS> struct TGShape {
     static constexpr int B_BYTES = NP * KC * 4;
     static constexpr int A_T = MS * A_BYTES;
     static constexpr int STAGE = A_T + 2 * B_BYTES;          // A (FP32 -> TF32 hi in place), B hi, B lo
-    static constexpr int NS = 3 * STAGE + 2 * A_T + 1100 <= 232448 ? 3 : 2;
-    static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 2 * A_T + 2 * NS * 8 + 16;
+    static constexpr size_t smem_for(int ns) { return 1024 + (size_t)ns * STAGE + 2 * A_T + 2 * ns * 8 + 16; }
+    static constexpr int NS = smem_for(6) <= 232448   ? 6
+                              : smem_for(5) <= 232448 ? 5
+                              : smem_for(4) <= 232448 ? 4
+                              : smem_for(3) <= 232448 ? 3
+                                                      : 2;
+    static constexpr size_t SMEM = smem_for(NS);
     static constexpr bool fits = SMEM <= 232448;
 };
 
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(160, 1)
                 const uint32_t bh_a = smem_u32(bh_st(s)), bl_a = smem_u32(bl_st(s));
 #pragma unroll
                 for (int j = 0; j < KC / 8; ++j) {
-                    const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the swizzled row
+                    const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the 64-byte swizzled row
                     const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
 #pragma unroll
                     for (int t = 0; t < MS; ++t) {   // sub-tile t: A rows 128 t.., accumulator columns 256 t..
@@ -322,7 +331,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2D FP32 tensor map: inner extent `inner` (elements), `outer` rows of pitch
-// `pitch` elements, box 32 x box_rows, 128-byte swizzle, zero fill outside
+// `pitch` elements, box KC x box_rows, 64-byte swizzle, zero fill outside
 void make_map(CUtensorMap *map, const void *ptr, uint64_t inner, uint64_t outer, uint64_t pitch, uint32_t box_rows) {
     TDZ_CHECK((reinterpret_cast<uintptr_t>(ptr) & 15) == 0, TDZ_ERR_ARG, "transform operand not 16-byte aligned");
     TDZ_CHECK((pitch * 4) % 16 == 0, TDZ_ERR_ARG, "transform row pitch not a multiple of 16 bytes");
@@ -331,7 +340,7 @@ void make_map(CUtensorMap *map, const void *ptr, uint64_t inner, uint64_t outer,
     const cuuint32_t box[2] = {(cuuint32_t)KC, box_rows};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(ptr), dims, strides,
-                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     TDZ_CHECK(r == CUDA_SUCCESS, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }

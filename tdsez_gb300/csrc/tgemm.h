@@ -21,7 +21,7 @@
 namespace tdz {
 
 // B split into TF32 hi + lo parts, K-major ([n][k]), zero-padded to Kp
-// (multiple of 32) and Np (multiple of 16, at most 256), stored [2][Np][Kp].
+// (multiple of 16) and Np (multiple of 16, at most 256), stored [2][Np][Kp].
 struct TransformMat {
     int K = 0, N = 0, Kp = 0, Np = 0;
     DevBuf hilo;
