@@ -126,12 +126,42 @@ void launch_1d(const ApplyParams<T> &prm, cudaStream_t st) {
 
 }  // namespace
 
+// sum of the fused-reduction partials, one block, fixed order
+__global__ void k_apply_red_finish(const double2 *part, int n, double2 *out) {
+    __shared__ double2 s[256];
+    double2 t = make_double2(0.0, 0.0);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        t.x += part[i].x;
+        t.y += part[i].y;
+    }
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            s[threadIdx.x].x += s[threadIdx.x + h].x;
+            s[threadIdx.x].y += s[threadIdx.x + h].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+void apply_red_finish(const double2 *part, double2 *out, cudaStream_t st) {
+    k_apply_red_finish<<<1, 256, 0, st>>>(part, kApplyRedCap, out);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
+}
+
 void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st,
-                  const void *sub) {
+                  const ApplyExtra &ex) {
     const int dim = op.sp->dim;
+    TDZ_CHECK(!ex.red_mode || dim == 3, TDZ_ERR_INTERNAL, "fused reductions are 3D only");
     auto params = [&](auto tag) {
         auto prm = make_params<decltype(tag)>(op, pl, x, y);
-        prm.sub = sub;
+        prm.sub = ex.sub;
+        prm.red = ex.red;
+        prm.dotv = ex.dotv;
+        prm.red_mode = ex.red_mode;
         return prm;
     };
     if (dim == 1) {

@@ -49,7 +49,13 @@ template <class T> struct ApplyParams {
     int walls;
     int za_kind, zc_kind;       // outer combinations: 0 complex, 1 real, 2 imaginary (fewer products)
     const void *sub;            // non-null: y = sub - op x (a residual), same layout as y
+    // 3D only: per-CTA partial sums of the stored y, red[blockIdx.x] (FP64):
+    // red_mode 1: sum |y|^2, 2: sum conj(dotv) y (dotv laid out as y)
+    double2 *red;
+    const void *dotv;
+    int red_mode;
 };
+
 
 // the value stored at output element e: op x, or sub[e] - op x
 template <class T, class MC, class C>
@@ -91,7 +97,7 @@ template <class T> constexpr bool kShiftRing = !std::is_same<T, float>::value;
 // the double-float CN stage (KC = 2) and mass (KA = 1) get their own
 // instantiations, which save a quarter of the outer-stage products.
 template <class T, int P, bool HB, bool HC, int TX, int TY, int KA, int KC>
-__device__ __noinline__ void apply3d_run(const ApplyParams<T> &prm, int x0, int y0, int z0, int z1) {
+__device__ __noinline__ double2 apply3d_run(const ApplyParams<T> &prm, int x0, int y0, int z0, int z1) {
     using C = typename CT<T>::type;
     constexpr int BW = 2 * P + 1, RY = TY + 2 * P, RX = TX + 2 * P;
     constexpr int NU = 1 + (HB ? 1 : 0) + (HC ? 1 : 0);
@@ -259,12 +265,21 @@ __device__ __noinline__ void apply3d_run(const ApplyParams<T> &prm, int x0, int 
         fetch(lo + 2);
         __syncthreads();
     }
+    double2 racc = make_double2(0.0, 0.0);   // this thread's share of the requested sum
     auto finish = [&](int it, C &out) {   // output plane zs + it - P is complete
         if (it >= 2 * P) {
             const int m = zs + it - P;
             if (gx < n0 && gy < n1) {
                 const size_t e = ((size_t)m * n1 + gy) * n0 + gx;
-                Y[e] = out_value<T, MC>(prm, e, out);
+                const MC v = out_value<T, MC>(prm, e, out);
+                Y[e] = v;
+                if (prm.red_mode == 1) {
+                    racc.x = fma((double)v.x, (double)v.x, fma((double)v.y, (double)v.y, racc.x));
+                } else if (prm.red_mode == 2) {
+                    const MC d = static_cast<const MC *>(prm.dotv)[e];
+                    racc.x = fma((double)d.x, (double)v.x, fma((double)d.y, (double)v.y, racc.x));
+                    racc.y = fma((double)d.x, (double)v.y, fma(-(double)d.y, (double)v.x, racc.y));
+                }
             }
         }
     };
@@ -295,6 +310,7 @@ __device__ __noinline__ void apply3d_run(const ApplyParams<T> &prm, int x0, int 
             }
         }
     }
+    return racc;
 }
 
 // This CTA owns planes [b L, (b + 1) L) of the (tile, z) order, z fastest
@@ -311,13 +327,32 @@ __global__ void __launch_bounds__(TX *TY) k_apply3d(const __grid_constant__ Appl
     const long long total = (long long)tilesX * ((n1 + TY - 1) / TY) * n2;
     long long pos = (long long)blockIdx.x * prm.zchunk;
     const long long end = min(total, pos + prm.zchunk);
+    double2 racc = make_double2(0.0, 0.0);
     for (bool first = true; pos < end; first = false) {
         const int tile = (int)(pos / n2);
         const int z0 = (int)(pos - (long long)tile * n2);
         const int z1 = (int)min((long long)n2, z0 + (end - pos));
         pos += z1 - z0;
         if (!first) __syncthreads();   // the last run's readers of the band rows are done
-        apply3d_run<T, P, HB, HC, TX, TY, KA, KC>(prm, (tile % tilesX) * txw, (tile / tilesX) * TY, z0, z1);
+        const double2 r =
+            apply3d_run<T, P, HB, HC, TX, TY, KA, KC>(prm, (tile % tilesX) * txw, (tile / tilesX) * TY, z0, z1);
+        racc.x += r.x;
+        racc.y += r.y;
+    }
+    if (prm.red_mode) {   // CTA sum -> red[blockIdx.x] (fixed order: deterministic)
+        __shared__ double2 wsum[32];
+        for (int off = 16; off > 0; off >>= 1) {
+            racc.x += __shfl_down_sync(0xffffffffu, racc.x, off);
+            racc.y += __shfl_down_sync(0xffffffffu, racc.y, off);
+        }
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x, nw = (blockDim.x * blockDim.y + 31) / 32;
+        if ((tid & 31) == 0) wsum[tid >> 5] = racc;
+        __syncthreads();
+        if (tid == 0) {
+            double2 t = make_double2(0.0, 0.0);
+            for (int w = 0; w < nw; ++w) { t.x += wsum[w].x; t.y += wsum[w].y; }
+            prm.red[blockIdx.x] = t;
+        }
     }
 }
 
@@ -537,6 +572,7 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
         prm.zchunk_planes = std::min(seg, n2) + 2 * P;
         const long long total = (long long)tiles_for(txw) * n2;
         const unsigned grid = (unsigned)((total + seg - 1) / seg);
+        TDZ_CHECK(!prm.red_mode || grid <= (unsigned)kApplyRedCap, TDZ_ERR_INTERNAL, "apply reduction slots");
         ensure_smem(smem_for(std::min(seg, n2)));
         kern<<<grid, dim3(txw, TY), smem_for(std::min(seg, n2)), st>>>(prm);
     };

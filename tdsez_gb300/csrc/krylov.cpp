@@ -30,10 +30,10 @@ void FGMRES::setup(Operator *op_, int restart_, Precond *pc_) {
     red.init();
 }
 
-SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st) {
+SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm_in) {
     SolveStats s;
     const int m = restart;
-    const double bnorm = blas::nrm2(red, b, n, TDZ_FP64, st);
+    const double bnorm = bnorm_in >= 0.0 ? bnorm_in : blas::nrm2(red, b, n, TDZ_FP64, st);
     s.bnorm = bnorm;
     if (!std::isfinite(bnorm)) {
         s.reason = -9;
@@ -49,7 +49,15 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     }
     const double target = rtol * bnorm;
     std::vector<cd> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), h(m + 1), h2(m + 1), y(m);
+    std::vector<cd> dts(m + 1), hc(m + 1), yc(m);
     std::vector<double> wn(m, 0.0);     // ||A z_j|| of relaxed columns (0 for exact ones)
+    // Stored units: V[0] keeps the unnormalised residual r0 = beta v0 (scale
+    // vsc[0] = 1/beta; V[j >= 1] are unit vectors), so no pass normalises it.
+    // Z[0] = P^-1 r0 stands for the direction z0 = Z[0] / beta, and the first
+    // Arnoldi vector w = A Z[0] for beta A z0 (ws = beta). The Hessenberg
+    // entries are kept in true units; the update coefficients of a pass over
+    // stored vectors carry the scales.
+    std::vector<double> vsc(m + 1, 1.0);
     std::vector<const void *> Vp(m + 1), Zp(m);
     for (int i = 0; i <= m; ++i) Vp[i] = V[i].ptr;
     for (int i = 0; i < m; ++i) Zp[i] = Z[i].ptr;
@@ -57,11 +65,11 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     bool used_relaxed = false, relax = relaxed;
     double beta_prev = -1.0;
     while (true) {
-        // r = b - A x  -> V0
+        // r = b - A x -> V0, with ||r|| from the same pass where the operator fuses it
         double2 *v0 = V[0].as<double2>();
-        op->residual(TDZ_STAGE, aprec, x, b, v0, st);
+        double beta = 0.0;
+        op->residual(TDZ_STAGE, aprec, x, b, v0, st, &beta);
         ++applies;
-        const double beta = blas::nrm2(red, v0, n, TDZ_FP64, st);
         if (!std::isfinite(beta)) { s.reason = -9; s.rnorm = beta; break; }
         s.rnorm = beta;
         if (beta <= target) { s.reason = 2; break; }
@@ -71,7 +79,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         used_relaxed = false;
         beta_prev = beta;
         if (total >= maxit) { s.reason = -3; break; }
-        blas::scale(v0, 1.0 / beta, n, TDZ_FP64, st);
+        vsc[0] = 1.0 / beta;
         std::fill(g.begin(), g.end(), cd(0));
         g[0] = beta;
         int j = 0;
@@ -81,25 +89,40 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             double2 *zj = Z[j].as<double2>();
             pc->apply(V[j].as<double2>(), zj, st);
             double2 *wv = w.as<double2>();
+            const double ws = j == 0 ? beta : 1.0;   // stored w = ws A z_j
+            bool have_dots = false;
             if (relax) {
                 blas::cast(zj, TDZ_FP64, z32.ptr, TDZ_FP32, n, st);
                 op->apply(TDZ_STAGE, TDZ_FP32, z32.ptr, w32.ptr, st);
                 blas::cast(w32.ptr, TDZ_FP32, wv, TDZ_FP64, n, st);
                 ++relaxed_applies;
                 used_relaxed = true;
+            } else if (j == 0) {
+                op->apply_dot(TDZ_STAGE, aprec, zj, wv, V[0].ptr, &dts[0], st);   // <V0, w> from the apply
+                have_dots = true;
             } else {
                 op->apply(TDZ_STAGE, aprec, zj, wv, st);
             }
             ++applies;
+            if (!have_dots) blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, dts.data(), st);
             // CGS with one re-orthogonalisation; up to 16 basis vectors the
-            // update and the next reduction share one pass over V and w
+            // update and the next reduction share one pass over V and w.
+            // h, h2: negated projections (true units); hc: their stored-unit
+            // coefficients
+            auto to_true = [&](std::vector<cd> &out) {
+                for (int i = 0; i <= j; ++i) out[i] = -(dts[i] * (vsc[i] / ws));
+            };
+            auto to_stored = [&](const std::vector<cd> &in) {
+                for (int i = 0; i <= j; ++i) hc[i] = in[i] * (ws * vsc[i]);
+            };
             double hn = 0.0;
-            blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h.data(), st);
-            for (int i = 0; i <= j; ++i) h[i] = -h[i];
+            to_true(h);
+            to_stored(h);
             if (j + 1 <= 16) {
                 double w1 = 0.0;
-                blas::gs_update(red, wv, j + 1, Vp.data(), h.data(), n, h2.data(), &w1, st);
-                for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
+                blas::gs_update(red, wv, j + 1, Vp.data(), hc.data(), n, dts.data(), &w1, st);
+                to_true(h2);
+                w1 /= ws;
                 // The second pass only restores the orthogonality of w for the
                 // next basis vector. If the least-squares residual with this
                 // column already meets the target (with a 2x margin), the
@@ -129,13 +152,18 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
                         ++early_accepts;
                     }
                 }
-                if (!early) blas::gs_update(red, wv, j + 1, Vp.data(), h2.data(), n, nullptr, &hn, st);
+                if (!early) {
+                    to_stored(h2);
+                    blas::gs_update(red, wv, j + 1, Vp.data(), hc.data(), n, nullptr, &hn, st);
+                    hn /= ws;
+                }
             } else {
-                blas::maxpy(wv, j + 1, Vp.data(), h.data(), n, TDZ_FP64, st);
-                blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, h2.data(), st);
-                for (int i = 0; i <= j; ++i) h2[i] = -h2[i];
-                blas::maxpy(wv, j + 1, Vp.data(), h2.data(), n, TDZ_FP64, st);
-                hn = blas::nrm2(red, wv, n, TDZ_FP64, st);
+                blas::maxpy(wv, j + 1, Vp.data(), hc.data(), n, TDZ_FP64, st);
+                blas::mdot(red, Vp.data(), j + 1, wv, n, TDZ_FP64, dts.data(), st);
+                to_true(h2);
+                to_stored(h2);
+                blas::maxpy(wv, j + 1, Vp.data(), hc.data(), n, TDZ_FP64, st);
+                hn = blas::nrm2(red, wv, n, TDZ_FP64, st) / ws;
             }
             for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = -(h[i] + h2[i]);
             if (!std::isfinite(hn)) { s.reason = -9; done = true; break; }
@@ -164,18 +192,21 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             g[j] = std::conj(cs[j]) * g[j];
             s.rnorm = std::abs(g[j + 1]);
             const bool last_col = (j + 1 == m) || total >= maxit;
-            if (hn > 0.0 && !(s.rnorm <= target) && !last_col)
-                blas::axpby(V[j + 1].ptr, cd(1.0 / hn), wv, 0.0, n, TDZ_FP64, st);
+            if (hn > 0.0 && !(s.rnorm <= target) && !last_col) {
+                blas::axpby(V[j + 1].ptr, cd(1.0 / (ws * hn)), wv, 0.0, n, TDZ_FP64, st);
+                vsc[j + 1] = 1.0;
+            }
             if (s.rnorm <= target || hn == 0.0) { ++j; done = true; break; }
         }
-        // x += Z y, y from the upper triangular system H y = g
+        // x += sum_i y_i z_i with z_0 = Z[0] / beta; y from H y = g
         const int k = j;
         for (int i = k - 1; i >= 0; --i) {
             cd acc = g[i];
             for (int l = i + 1; l < k; ++l) acc -= H[(size_t)i * m + l] * y[l];
             y[i] = acc / H[(size_t)i * m + i];
         }
-        if (k > 0) blas::maxpy(x, k, Zp.data(), y.data(), n, TDZ_FP64, st);
+        for (int i = 0; i < k; ++i) yc[i] = i == 0 ? y[i] / beta : y[i];
+        if (k > 0) blas::maxpy(x, k, Zp.data(), yc.data(), n, TDZ_FP64, st);
         if (s.reason == -9) break;
         if (done && s.rnorm <= target) {
             // relaxed applies: accept when the bound on the gap between the

@@ -61,7 +61,8 @@ struct FGMRES {
 
     void setup(Operator *op_, int restart_, Precond *pc_);
     // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.
-    SolveStats solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st);
+    // bnorm: ||b|| when the caller has it (< 0: computed here)
+    SolveStats solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm = -1.0);
 };
 
 }  // namespace tdz

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <map>
 
 namespace tdz {
@@ -261,20 +262,80 @@ void Operator::set_stage(cd alpha, cd g, const std::vector<cd> &c) {
 
 void Operator::apply(int which, int prec, const void *x, void *y, cudaStream_t st) { residual(which, prec, x, nullptr, y, st); }
 
-void Operator::residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st) {
+bool Operator::fused_reductions() const { return sp->dim == 3 && !quad.on; }
+
+namespace {
+// one fused-reduction result to the host (synchronises the stream)
+cd take_reduction(Operator &op, cudaStream_t st) {
+    apply_red_finish(op.red_part.as<double2>(), op.red_res.as<double2>(), st);
+    double2 v;
+    TDZ_CUDA(cudaMemcpyAsync(&v, op.red_res.ptr, sizeof(double2), cudaMemcpyDeviceToHost, st));
+    TDZ_CUDA(cudaStreamSynchronize(st));
+    return cd(v.x, v.y);
+}
+void ensure_red(Operator &op) {
+    if (op.red_part.ptr) return;
+    op.red_part.alloc(sizeof(double2) * kApplyRedCap);
+    op.red_res.alloc(sizeof(double2));
+}
+}  // namespace
+
+void Operator::residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st, double *norm) {
     TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG,
               "precision must be TDZ_FP32, TDZ_FP64 or TDZ_FP64_DF");
     TDZ_CHECK(x && y, TDZ_ERR_ARG, "null vector");
     TDZ_CHECK(x != y, TDZ_ERR_ARG, "x and y must not alias");
     if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");
     Plan &pl = plan(which);
-    launch_apply(*this, pl, prec, x, y, st, b);
+    ApplyExtra ex;
+    ex.sub = b;
+    const bool fused = norm && fused_reductions();
+    if (fused) {
+        ensure_red(*this);
+        TDZ_CUDA(cudaMemsetAsync(red_part.ptr, 0, sizeof(double2) * kApplyRedCap, st));
+        ex.red = red_part.as<double2>();
+        ex.red_mode = 1;
+    }
+    launch_apply(*this, pl, prec, x, y, st, ex);
     if (quad.on && (which == TDZ_HAMILTONIAN || which == TDZ_STAGE)) {
         // y += s (g for the stage) V_q x; minus that for a residual
         const cd coef = -phys.charge * (which == TDZ_STAGE ? sigma[1] : cd(1.0));
         quad.apply(b ? -coef : coef, prec, x, y, st);
     }
     ++launches;
+    if (norm) {
+        if (fused) {
+            const double v = take_reduction(*this, st).real();
+            *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
+        } else {
+            blas::Reducer red;
+            *norm = blas::nrm2(red, y, (size_t)sp->ndof(), prec == TDZ_FP32 ? TDZ_FP32 : TDZ_FP64, st);
+        }
+    }
+}
+
+void Operator::apply_dot(int which, int prec, const void *x, void *y, const void *v, cd *dot, cudaStream_t st) {
+    TDZ_CHECK(prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG, "apply_dot works on FP64 vectors");
+    if (!fused_reductions()) {
+        apply(which, prec, x, y, st);
+        blas::Reducer red;
+        const void *V[1] = {v};
+        blas::mdot(red, V, 1, y, (size_t)sp->ndof(), TDZ_FP64, dot, st);
+        return;
+    }
+    TDZ_CHECK(x && y && v, TDZ_ERR_ARG, "null vector");
+    TDZ_CHECK(x != y, TDZ_ERR_ARG, "x and y must not alias");
+    if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");
+    Plan &pl = plan(which);
+    ensure_red(*this);
+    TDZ_CUDA(cudaMemsetAsync(red_part.ptr, 0, sizeof(double2) * kApplyRedCap, st));
+    ApplyExtra ex;
+    ex.red = red_part.as<double2>();
+    ex.dotv = v;
+    ex.red_mode = 2;
+    launch_apply(*this, pl, prec, x, y, st, ex);
+    ++launches;
+    *dot = take_reduction(*this, st);
 }
 
 void Operator::observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st) {

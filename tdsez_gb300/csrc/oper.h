@@ -75,8 +75,15 @@ struct Operator {
     void compile(Plan &pl, const std::vector<Term> &ts) const;
     void set_stage(cd alpha, cd g, const std::vector<cd> &c);
     void apply(int which, int prec, const void *x, void *y, cudaStream_t st);
-    // y = b - op x in one pass (b and y FP64 for TDZ_FP64 / TDZ_FP64_DF)
-    void residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st);
+    // y = b - op x in one pass (b and y FP64 for TDZ_FP64 / TDZ_FP64_DF);
+    // b may be null (y = op x). With norm: *norm = ||y|| (fused into the
+    // store for 3D operators without the quadrature term; synchronises)
+    void residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st,
+                  double *norm = nullptr);
+    // y = op x and *dot = <v, y> = sum conj(v) y (FP64 vectors; synchronises)
+    void apply_dot(int which, int prec, const void *x, void *y, const void *v, cd *dot, cudaStream_t st);
+    DevBuf red_part, red_res;      // fused-reduction partials and result
+    bool fused_reductions() const;
     // <psi|M|psi>, <psi|H|psi>, <psi|D_a|psi> (FP64 psi); see tdz_observables
     std::vector<DevBuf> obs_buf;
     void observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
@@ -89,8 +96,19 @@ enum BaseId { kM = 0, kS = 1, kX = 2 };
 void set_autotune(int on);
 
 // kernel launchers (apply.cu)
-// y = op x, or y = sub - op x when sub is non-null (the residual, fused into the store)
+// Extras of one apply, fused into its store: y = sub - op x when sub is
+// non-null (a residual); for 3D, per-CTA partial sums of |y|^2 (red_mode 1)
+// or of conj(dotv) y (red_mode 2) into red[0 .. kApplyRedCap).
+constexpr int kApplyRedCap = 4096;   // partial-sum slots (CTAs of one 3D launch)
+// red[0 .. kApplyRedCap) summed into *out (device), fixed order
+void apply_red_finish(const double2 *part, double2 *out, cudaStream_t st);
+struct ApplyExtra {
+    const void *sub = nullptr;
+    double2 *red = nullptr;
+    const void *dotv = nullptr;
+    int red_mode = 0;
+};
 void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st,
-                  const void *sub = nullptr);
+                  const ApplyExtra &ex = ApplyExtra{});
 
 }  // namespace tdz

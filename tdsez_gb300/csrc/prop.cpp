@@ -69,8 +69,8 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
     ksp.aprec = o.outer;
 }
 
-SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st) {
-    SolveStats s = ksp.solve(b, x, opt.rtol, opt.maxit, st);
+SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st, double bnorm) {
+    SolveStats s = ksp.solve(b, x, opt.rtol, opt.maxit, st, bnorm);
     if (opt.pc == 3 && static_cast<PcFDM *>(pc.get())->tensor)
         TDZ_CHECK(take_transform_error() == 0, TDZ_ERR_CUDA, "tensor-core transform: a bounded wait ran out");
     ++solves;
@@ -118,8 +118,8 @@ void Propagator::record(int slot, const double2 *y, const double2 *x, cudaStream
     hist_count[slot] = std::min(hist_count[slot] + 1, guess_order);
 }
 
-void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st) {
-    SolveStats s = solver[k].solve(b, x, st);
+void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st, double bnorm) {
+    SolveStats s = solver[k].solve(b, x, st, bnorm);
     last = s;
     ++solves;
     its += s.its;
@@ -134,7 +134,8 @@ void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t s
 
 void Propagator::cn_step(double2 *psi, double h, const std::vector<cd> &c, cudaStream_t st) {
     op->set_stage(1.0, cd(0.0, 0.5 * h), c);
-    op->apply(TDZ_MASS, aprec, psi, rhs.ptr, st);          // M psi
+    double bn = -1.0;
+    op->residual(TDZ_MASS, aprec, psi, nullptr, rhs.ptr, st, op->fused_reductions() ? &bn : nullptr);   // M psi
     double2 *X = tmp.as<double2>();
     if (guess_order < 0) {
         solver[0].pc->apply(rhs.as<double2>(), X, st);           // x0 = P^-1 b
@@ -142,7 +143,7 @@ void Propagator::cn_step(double2 *psi, double h, const std::vector<cd> &c, cudaS
         blas::copy(psi, X, n, TDZ_FP64, st);
         extrapolate(0, X, st);
     }
-    stage_solve(0, rhs.as<double2>(), X, st);
+    stage_solve(0, rhs.as<double2>(), X, st, bn);
     record(0, X, psi, st);
     blas::axpby(psi, 2.0, X, -1.0, n, TDZ_FP64, st);           // psi <- 2 X - psi
 }
