@@ -343,8 +343,8 @@ def run_tdz(args):
                      "frac": bytes64 / tdf / 1e9 / pk.get("hbm_gbs", 6800.0), "traffic": DF_APPLY_TRAFFIC,
                      "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
                      "launch_us": tdf * 1e6, "bytes_per_launch": bytes64,
-                     "limiter": "FP32 pipes: 12 FP32 instructions per double-float FMA (ncu: 50.6% issue, "
-                                "42.8% FMA pipe)",
+                     "limiter": "FP32 pipes: 12 FP32 instructions per double-float FMA (ncu: 64.8% issue, "
+                                "52.1% FMA pipe)",
                      "fp32_apply": {"kernel": "k_apply3d<float> (multigrid smoother and residual)",
                                     "achieved": ach32, "frac": ach32 / pk.get("hbm_gbs", 6800.0),
                                     "launch_us": t32 * 1e6, "bytes_per_launch": bytes32},
@@ -364,8 +364,10 @@ def run_tdz(args):
 
 CPU_GRID = (16, 16, 32)
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_apply3d<dff,3,0,1> launch on the
-# 160x160x320 workload (ncu --set full, profiles/k_apply3d_df_stage_heterostructure_160x160x320_p3.md)
-DF_APPLY_TRAFFIC = 146.86e6 + 99.14e6
+# 160x160x320 workload at its tuned launch shape (16 x 16 tiles, 303 CTAs; ncu --set full,
+# profiles/k_apply3d_df_stage_heterostructure_160x160x320_p3.md). The narrow tiles re-read
+# their x / y halos, which the FP32-pipe-bound kernel can afford.
+DF_APPLY_TRAFFIC = 297.75e6 + 125.24e6
 
 
 def apply_only(args, op, S, psi0, stream):
