@@ -67,6 +67,16 @@ __device__ __forceinline__ MC out_value(const ApplyParams<T> &prm, size_t e, C v
     }
     return store_c<MC>(v);
 }
+// the same with sub[e] already loaded
+template <class T, class MC, class C>
+__device__ __forceinline__ MC out_value_sub(const ApplyParams<T> &prm, MC b, C v) {
+    if (prm.sub) {
+        C r = load_c<C>(b);
+        rfma(r, T(-1.f), v);
+        v = cnorm(r);
+    }
+    return store_c<MC>(v);
+}
 
 // entry o of row i of a combination of base bands
 template <class T, class C>
@@ -266,17 +276,29 @@ __device__ __noinline__ double2 apply3d_run(const ApplyParams<T> &prm, int x0, i
         __syncthreads();
     }
     double2 racc = make_double2(0.0, 0.0);   // this thread's share of the requested sum
-    auto finish = [&](int it, C &out) {   // output plane zs + it - P is complete
+    // The side input of output plane zs + it - P (sub for a residual, else dotv
+    // for a dot) is requested before the plane's step, so its latency overlaps
+    // the step's compute.
+    auto side_load = [&](int it) {
+        MC sv{};
+        if (it >= 2 * P && gx < n0 && gy < n1) {
+            const size_t e = ((size_t)(zs + it - P) * n1 + gy) * n0 + gx;
+            if (prm.sub) sv = static_cast<const MC *>(prm.sub)[e];
+            else if (prm.red_mode == 2) sv = static_cast<const MC *>(prm.dotv)[e];
+        }
+        return sv;
+    };
+    auto finish = [&](int it, C &out, MC sv) {   // output plane zs + it - P is complete
         if (it >= 2 * P) {
             const int m = zs + it - P;
             if (gx < n0 && gy < n1) {
                 const size_t e = ((size_t)m * n1 + gy) * n0 + gx;
-                const MC v = out_value<T, MC>(prm, e, out);
+                const MC v = out_value_sub<T, MC>(prm, sv, out);
                 Y[e] = v;
                 if (prm.red_mode == 1) {
                     racc.x = fma((double)v.x, (double)v.x, fma((double)v.y, (double)v.y, racc.x));
                 } else if (prm.red_mode == 2) {
-                    const MC d = static_cast<const MC *>(prm.dotv)[e];
+                    const MC d = prm.sub ? static_cast<const MC *>(prm.dotv)[e] : sv;
                     racc.x = fma((double)d.x, (double)v.x, fma((double)d.y, (double)v.y, racc.x));
                     racc.y = fma((double)d.x, (double)v.y, fma(-(double)d.y, (double)v.x, racc.y));
                 }
@@ -290,8 +312,9 @@ __device__ __noinline__ double2 apply3d_run(const ApplyParams<T> &prm, int x0, i
         // emulated-FP64 body inside the instruction cache
 #pragma unroll 1
         for (int it = 0; it < nplanes; ++it) {
+            const MC sv = side_load(it);
             if (it >= lo && it < hi) step(it, 0);
-            finish(it, acc[0]);
+            finish(it, acc[0], sv);
 #pragma unroll
             for (int s = 0; s + 1 < BW; ++s) acc[s] = acc[s + 1];
             acc[BW - 1] = czero<C>();
@@ -304,8 +327,9 @@ __device__ __noinline__ double2 apply3d_run(const ApplyParams<T> &prm, int x0, i
                 const int it = base + ph;
                 if (it >= nplanes) break;
                 const int ring = (ph - P + 2 * BW) % BW;
+                const MC sv = side_load(it);
                 if (it >= lo && it < hi) step(it, ring);
-                finish(it, acc[ring]);
+                finish(it, acc[ring], sv);
                 acc[ring] = czero<C>();
             }
         }

@@ -148,6 +148,17 @@ __global__ void k_axpbypcz_r64(double2 *y, double a, const double2 *x, double b,
     }
 }
 
+// psi = 2 x - psi + c z: the CN state update fused with the last FGMRES
+// correction (c z in double-float, the rest in FP64)
+__global__ void k_cn_combine(double2 *psi, const double2 *x, const double2 *z, cdff c, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        cdff t = czero<cdff>();
+        cfma(t, c, ld_df(z[i]));
+        const double2 xv = x[i], pv = psi[i];
+        psi[i] = make_double2(fma(2.0, xv.x, -pv.x) + dff_to_double(t.x), fma(2.0, xv.y, -pv.y) + dff_to_double(t.y));
+    }
+}
+
 __global__ void k_scale_r64(double2 *x, double a, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double2 v = x[i];
@@ -526,6 +537,14 @@ void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, si
         const double v = r.host[nres - 1].x;
         *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
     }
+}
+
+void cn_combine(void *psi, const void *x, const void *z, cd c, size_t n, cudaStream_t st) {
+    const int g = (int)std::min<size_t>((n + kThreads - 1) / kThreads, (size_t)kRedBlocks);
+    k_cn_combine<<<g, kThreads, 0, st>>>(static_cast<double2 *>(psi), static_cast<const double2 *>(x),
+                                         static_cast<const double2 *>(z), cdf_host(c), n);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st) {

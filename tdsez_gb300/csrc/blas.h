@@ -47,6 +47,8 @@ void mdot_partials(const void *const *V, int k, const void *w, size_t n, int pre
 constexpr int kRedBlocksPublic = 2 * 152;   // blocks of the reductions (partials per dot product)
 // w += sum_i a_i V_i
 void maxpy(void *w, int k, const void *const *V, const cd *a, size_t n, int prec, cudaStream_t st);
+// FP64 psi = 2 x - psi + c z (Crank-Nicolson update with the last Krylov correction)
+void cn_combine(void *psi, const void *x, const void *z, cd c, size_t n, cudaStream_t st);
 // ||x||_2 (synchronises)
 double nrm2(Reducer &r, const void *x, size_t n, int prec, cudaStream_t st);
 // FP64 Arnoldi vector, fused Gram-Schmidt pass (k <= 16): w += sum_i a_i V_i,

@@ -30,8 +30,10 @@ void FGMRES::setup(Operator *op_, int restart_, Precond *pc_) {
     red.init();
 }
 
-SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm_in) {
+SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm_in,
+                         double2 *cn_psi, bool *cn_done) {
     SolveStats s;
+    if (cn_done) *cn_done = false;
     const int m = restart;
     const double bnorm = bnorm_in >= 0.0 ? bnorm_in : blas::nrm2(red, b, n, TDZ_FP64, st);
     s.bnorm = bnorm;
@@ -206,7 +208,13 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
             y[i] = acc / H[(size_t)i * m + i];
         }
         for (int i = 0; i < k; ++i) yc[i] = i == 0 ? y[i] / beta : y[i];
-        if (k > 0) blas::maxpy(x, k, Zp.data(), yc.data(), n, TDZ_FP64, st);
+        const bool final_one = cn_psi && k == 1 && done && s.rnorm <= target && !used_relaxed && s.reason != -9;
+        if (final_one) {
+            blas::cn_combine(cn_psi, x, Zp[0], 2.0 * yc[0], n, st);   // psi = 2 (x + yc Z0) - psi
+            *cn_done = true;
+        } else if (k > 0) {
+            blas::maxpy(x, k, Zp.data(), yc.data(), n, TDZ_FP64, st);
+        }
         if (s.reason == -9) break;
         if (done && s.rnorm <= target) {
             // relaxed applies: accept when the bound on the gap between the

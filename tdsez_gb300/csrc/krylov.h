@@ -61,8 +61,12 @@ struct FGMRES {
 
     void setup(Operator *op_, int restart_, Precond *pc_);
     // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.
-    // bnorm: ||b|| when the caller has it (< 0: computed here)
-    SolveStats solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm = -1.0);
+    // bnorm: ||b|| when the caller has it (< 0: computed here). cn_psi: when
+    // the solve converges after one iteration, its last update is fused with
+    // the Crank-Nicolson state update psi = 2 x - psi (*cn_done = true; x is
+    // then left at its initial guess); otherwise x is the solution as usual.
+    SolveStats solve(const double2 *b, double2 *x, double rtol, int maxit, cudaStream_t st, double bnorm = -1.0,
+                     double2 *cn_psi = nullptr, bool *cn_done = nullptr);
 };
 
 }  // namespace tdz

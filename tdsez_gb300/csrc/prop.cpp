@@ -69,8 +69,9 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
     ksp.aprec = o.outer;
 }
 
-SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st, double bnorm) {
-    SolveStats s = ksp.solve(b, x, opt.rtol, opt.maxit, st, bnorm);
+SolveStats Solver::solve(const double2 *b, double2 *x, cudaStream_t st, double bnorm, double2 *cn_psi,
+                         bool *cn_done) {
+    SolveStats s = ksp.solve(b, x, opt.rtol, opt.maxit, st, bnorm, cn_psi, cn_done);
     if (opt.pc == 3 && static_cast<PcFDM *>(pc.get())->tensor)
         TDZ_CHECK(take_transform_error() == 0, TDZ_ERR_CUDA, "tensor-core transform: a bounded wait ran out");
     ++solves;
@@ -118,8 +119,9 @@ void Propagator::record(int slot, const double2 *y, const double2 *x, cudaStream
     hist_count[slot] = std::min(hist_count[slot] + 1, guess_order);
 }
 
-void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st, double bnorm) {
-    SolveStats s = solver[k].solve(b, x, st, bnorm);
+void Propagator::stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st, double bnorm, double2 *cn_psi,
+                             bool *cn_done) {
+    SolveStats s = solver[k].solve(b, x, st, bnorm, cn_psi, cn_done);
     last = s;
     ++solves;
     its += s.its;
@@ -143,9 +145,14 @@ void Propagator::cn_step(double2 *psi, double h, const std::vector<cd> &c, cudaS
         blas::copy(psi, X, n, TDZ_FP64, st);
         extrapolate(0, X, st);
     }
-    stage_solve(0, rhs.as<double2>(), X, st, bn);
-    record(0, X, psi, st);
-    blas::axpby(psi, 2.0, X, -1.0, n, TDZ_FP64, st);           // psi <- 2 X - psi
+    // without extrapolation history X is not needed after the step: the last
+    // FGMRES update and psi <- 2 X - psi then share one pass
+    bool fused = false;
+    stage_solve(0, rhs.as<double2>(), X, st, bn, guess_order <= 0 ? psi : nullptr, &fused);
+    if (!fused) {
+        record(0, X, psi, st);
+        blas::axpby(psi, 2.0, X, -1.0, n, TDZ_FP64, st);       // psi <- 2 X - psi
+    }
 }
 
 void Propagator::pade_step(double2 *psi, double h, const std::vector<cd> &c, int slot, cudaStream_t st) {

@@ -40,8 +40,10 @@ struct Solver {
     FGMRES ksp;
     long long solves = 0, its = 0;
     void setup(Operator *op_, const SolverOptions &o, cudaStream_t st);
-    // bnorm: ||b|| when the caller has it (< 0: computed in the solve)
-    SolveStats solve(const double2 *b, double2 *x, cudaStream_t st, double bnorm = -1.0);
+    // bnorm: ||b|| when the caller has it (< 0: computed in the solve);
+    // cn_psi / cn_done: see FGMRES::solve
+    SolveStats solve(const double2 *b, double2 *x, cudaStream_t st, double bnorm = -1.0, double2 *cn_psi = nullptr,
+                     bool *cn_done = nullptr);
 };
 
 // Preconditioner refresh rule of TDSEZPCRefresh (include/tdsez_propagator.hpp:17-31):
@@ -82,7 +84,8 @@ struct Propagator {
   private:
     void extrapolate(int slot, double2 *psi, cudaStream_t st);
     void record(int slot, const double2 *y, const double2 *x, cudaStream_t st);
-    void stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st, double bnorm = -1.0);
+    void stage_solve(int k, const double2 *b, double2 *x, cudaStream_t st, double bnorm = -1.0,
+                     double2 *cn_psi = nullptr, bool *cn_done = nullptr);
 };
 
 }  // namespace tdz
