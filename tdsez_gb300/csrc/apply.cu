@@ -27,10 +27,6 @@ bool forced_shape(int *txw, int *run) {
     *run = b;
     return true;
 }
-bool smem_attr_exact() {
-    static const bool v = std::getenv("TDZ_APPLY3D_SMEM_EXACT") != nullptr;
-    return v;
-}
 bool tune_verbose() {
     static const bool v = std::getenv("TDZ_AUTOTUNE_VERBOSE") != nullptr;
     return v;

@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cstdio>
 #include <type_traits>
 #include <vector>
@@ -538,9 +537,6 @@ bool autotune_enabled();
 bool tune_verbose();   // TDZ_AUTOTUNE_VERBOSE set: the autotuner prints each candidate's time
 // TDZ_APPLY3D_SHAPE="tile_x,run": a fixed launch shape for every 3D apply (no autotuning)
 bool forced_shape(int *txw, int *run);
-// TDZ_APPLY3D_SMEM_EXACT set: raise the dynamic shared-memory limit of a 3D
-// apply kernel only as far as its launches need (default: one opt-in to 200 KB)
-bool smem_attr_exact();
 bool tune_lookup(const TuneKey &k, int *txw, int *zchunk);
 void tune_store(const TuneKey &k, int txw, int zchunk);
 
@@ -558,24 +554,15 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
     // shared memory grows with the run length (its band rows, at most n2 + 2p
     // planes): one opt-in to the largest size, occupancy at the largest size
     constexpr size_t kMaxDyn = 200 * 1024;
-    static int nsm = 0;
-    if (!nsm) {
-        if (!smem_attr_exact())
-            TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDyn));
-        int dev = 0;
+    static const int nsm = [&] {   // once per instantiation (thread-safe static initialisation)
+        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDyn));
+        int dev = 0, n = 0;
         TDZ_CUDA(cudaGetDevice(&dev));
-        TDZ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    }
+        TDZ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        return n;
+    }();
     const int n2 = prm0.n2;
     TDZ_CHECK(smem_for(n2) <= kMaxDyn, TDZ_ERR_UNSUPPORTED, "outer axis too long for the 3D apply");
-    static std::atomic<size_t> attr_set{0};
-    auto ensure_smem = [&](size_t need) {
-        if (!smem_attr_exact()) return;
-        size_t cur = attr_set.load();
-        if (need <= cur) return;
-        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-        attr_set.store(need);
-    };
     thread_local int occ_n2 = -1, occ_slots = 0;   // resident CTAs at the last n2 seen
     if (occ_n2 != n2) {
         int per_sm = 0;
@@ -590,14 +577,17 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
         const long long total = (long long)tiles_for(txw) * n2;
         return (int)std::min<long long>(total, std::max<long long>(4 * P, (total + g - 1) / g));
     };
-    auto launch = [&](int txw, int seg) {
+    // (tuning candidates run without the fused reduction; the final launch
+    // keeps its grid within the reduction's partial-sum slots)
+    auto launch = [&](int txw, int seg, bool candidate = false) {
         ApplyParams<T> prm = prm0;
+        const long long total = (long long)tiles_for(txw) * n2;
+        if (candidate) prm.red_mode = 0;
+        if (prm.red_mode) seg = (int)std::max<long long>(seg, (total + kApplyRedCap - 1) / kApplyRedCap);
         prm.zchunk = seg;
         prm.zchunk_planes = std::min(seg, n2) + 2 * P;
-        const long long total = (long long)tiles_for(txw) * n2;
         const unsigned grid = (unsigned)((total + seg - 1) / seg);
-        TDZ_CHECK(!prm.red_mode || grid <= (unsigned)kApplyRedCap, TDZ_ERR_INTERNAL, "apply reduction slots");
-        ensure_smem(smem_for(std::min(seg, n2)));
+        TDZ_CHECK(smem_for(std::min(seg, n2)) <= kMaxDyn, TDZ_ERR_UNSUPPORTED, "outer axis too long for the 3D apply");
         kern<<<grid, dim3(txw, TY), smem_for(std::min(seg, n2)), st>>>(prm);
     };
     // heuristic: one wave of persistent CTAs; FP32 full warps along x and two
@@ -622,10 +612,10 @@ inline void run3d(const ApplyParams<T> &prm0, cudaStream_t st) {
         TDZ_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         for (const auto &c : cand) {
-            launch(c.first, c.second);
+            launch(c.first, c.second, true);
             TDZ_CUDA(cudaEventRecord(e0, st));
-            launch(c.first, c.second);
-            launch(c.first, c.second);
+            launch(c.first, c.second, true);
+            launch(c.first, c.second, true);
             TDZ_CUDA(cudaEventRecord(e1, st));
             TDZ_CUDA(cudaEventSynchronize(e1));
             float ms = 0.f;
