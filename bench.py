@@ -319,7 +319,7 @@ def run_tdz(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 FGMRES) + c64 (FP32 multigrid)",
+        "scaling": "weak", "vs_baseline": None, "dtype": ("c128 (FP64 FGMRES, double-float applies) + c64 (FP32 " + args.pc + " preconditioner)"),
         "data": "synthetic (seeded heterostructure, Gaussian packet)",
         "config": {"workload": "3D heterostructure CN, 160x160x320 el, p=3, 5 C0 interfaces, N=%d" % N,
                    "global_batch": world, "dt": dt, "rtol": args.rtol, "precond": args.pc + " (FP32) in FP64 FGMRES",
@@ -420,7 +420,7 @@ def run_reference(args):
     n_full = 163 * 163 * 333
     cb = cpu_baseline(n_full, 0.5, args.cpu_seconds)
     v = cb["value"]
-    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "impl": "reference",
            "config": {"workload": "3D heterostructure CN, 160x160x320 el, p=3, 5 C0 interfaces, N=%d" % n_full},
            "cpu_baseline": {"kind": "port", "cores": 1, "sample": cb["sample"], "value": v},
