@@ -319,7 +319,9 @@ def run_tdz(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": ("c128 (FP64 FGMRES, double-float applies) + c64 (FP32 " + args.pc + " preconditioner)"),
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("c128 (FP64 FGMRES, " + ("double-float" if args.outer == "df" else "FP64") + " applies) + c64 (FP32 "
+                  + args.pc + " preconditioner)"),
         "data": "synthetic (seeded heterostructure, Gaussian packet)",
         "config": {"workload": "3D heterostructure CN, 160x160x320 el, p=3, 5 C0 interfaces, N=%d" % N,
                    "global_batch": world, "dt": dt, "rtol": args.rtol, "precond": args.pc + " (FP32) in FP64 FGMRES",
