@@ -7,10 +7,15 @@ stage solve (M + i dt/2 H_E) X = M psi to ||b - A X|| <= 1e-10 ||b|| in FP64
 (FGMRES) plus psi <- 2X - psi.
 
 Arms (same workload, same stopping rule):
-  value      mixed precision: FP64 FGMRES, FP32 geometric B-spline multigrid
+  value      FP64 FGMRES with double-float applies, FP32 fast-diagonalisation
+             preconditioner (--pc fdm, default), initial guess x0 = P^-1 b
+  mixed_mg   FP64 FGMRES, FP32 geometric B-spline multigrid
   plain_mg   the plain GPU multigrid form: the same multigrid in FP64
 e2e: the same steps through the C ABI with the state in pinned host memory,
 copied host->device before and device->host after every step.
+cpu_baseline / --impl reference: the reference's GMRES(30) + ILU(0) CPU
+method restated in C (oracle/cn_bjilu.c, OpenMP over the host cores) on a
+reduced grid, scaled by the coefficient count.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
