@@ -139,6 +139,13 @@ tdz_status tdz_operator_mass_solve(tdz_op *op, int precision, void *x, void *str
  * tile widths and z chunks on the caller's stream (CUDA events, about 30 ms
  * once) and keeps the fastest; with on = 0 a fixed heuristic picks them. */
 void tdz_set_autotune(int on);
+/* A fixed launch shape for every fused 3D apply: tile width tile_x (16..32,
+ * a multiple of 4) and run length `run` (z planes of the (tile, z) order per
+ * CTA, at least 4p); tile_x <= 0 or run <= 0 returns to autotuning. Also set
+ * by TDZ_APPLY3D_SHAPE="tile_x,run" in the environment at load time. For
+ * reproducing a measured shape and for parity tests at given launch shapes;
+ * no counterpart in the reference. */
+void tdz_set_apply3d_shape(int tile_x, int run);
 /* Observables of a state (FP64 device vector psi) in one call: the monitor
  * products of TDSEZManager::MonitorProducts (src/manager.cpp:584-672) reduced
  * to expectation values. out (host, 2 + 2 + 2 dim doubles):
@@ -192,6 +199,10 @@ typedef struct tdz_solver_opts {
                            to the true residual meets rtol (rnorm returns
                            that sum), else one more restart residual
                            decides                                           */
+    int pc_refresh_its; /* propagators: > 0 also rebuild the preconditioner
+                           whenever a stage solve takes more than this many
+                           iterations (-tdsez_pc_refresh_its); 0 = only the
+                           2 base + 5 rule of tdz_pc_refresh_stale           */
 } tdz_solver_opts;
 /* Set up the solver for the current stage of op (call set_stage first). */
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);
@@ -226,15 +237,16 @@ tdz_status tdz_solver_coarse_gain(tdz_solver *s, int trials, unsigned long long 
  * vectors), accumulated in FP64 by a deterministic two-pass reduction (the
  * VecDot of the Krylov and monitor paths, e.g. <psi|D|psi> after
  * tdz_operator_apply). out: one complex double (16 bytes) in device memory.
- * The per-block partial sums live in library-owned device scratch, allocated
- * on the first call on each device. */
+ * The per-block partial sums live in library-owned device scratch, one per
+ * (device, stream), allocated on the first call on that stream: calls on
+ * different streams may overlap, calls on one stream are ordered by it. */
 tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision, void *out, void *stream);
 
 /* out[i] = sum_j conj(V_i[j]) w[j] for i < k (any k): the fused multi-dot of
  * the classical Gram-Schmidt passes (VecMDot). V: host array of k device
  * vector pointers; out: k complex doubles in device memory. Same reduction
- * as tdz_vec_dot (library-owned scratch, allocated on first use per device;
- * chunks of 16 vectors per pass). */
+ * and the same per-(device, stream) scratch as tdz_vec_dot (chunks of 16
+ * vectors per pass). */
 tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n, int precision, void *out,
                         void *stream);
 
@@ -247,9 +259,14 @@ tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n,
  * until the process exits); at most 8 dot products per call, larger k is
  * rejected with TDZ_ERR_ARG. The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress); make it before any stream capture.
- * All calls share the array: calls that overlap on the GPU (different
- * streams, or different host threads on one device) race. Calls no
- * cudaMalloc / cudaFree and no allocating library routine. */
+ * With lazy module loading (CUDA_MODULE_LOADING=LAZY, the default) that
+ * first look-up may also load the library's device code onto the device,
+ * which the driver does without a cudaMalloc but with memory of its own.
+ * The address is then cached for the life of the device's primary context:
+ * after cudaDeviceReset the cache is stale, so do not call this entry point
+ * after a reset. All calls share the array: calls that overlap on the GPU
+ * (different streams, or different host threads on one device) race. Calls
+ * no cudaMalloc / cudaFree and no allocating library routine. */
 tdz_status tdz_vec_mdot_noalloc(const void *const *V, int k, const void *w, long long n, int precision, void *out,
                                 void *stream);
 
@@ -277,6 +294,8 @@ tdz_status tdz_plane_transform(const double *B, int K, int N, const float *in, i
  * (the PetscCheck(reason > 0) of src/propagator.cpp:671-672).
  */
 typedef struct tdz_prop tdz_prop;
+/* Physical field E_a(t) of axis a (0 on uncoupled axes), a host callback. */
+typedef double (*tdz_field_fn)(int axis, double t, void *ctx);
 #define TDZ_CN 0
 #define TDZ_PADE22 1
 #define TDZ_MAGNUS4 2
@@ -288,8 +307,6 @@ typedef struct tdz_prop tdz_prop;
 tdz_status tdz_prop_create(tdz_op *op, int kind, const tdz_solver_opts *opts, int guess_order, void *stream,
                            tdz_prop **out);
 tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, const double *c2, void *stream);
-/* Totals: stage solves, Krylov iterations, FP64 operator applies of the
- * solver, multigrid cycles; last solve's iterations and relative residual. */
 /* Batched steps: count independent propagations (each its own tdz_prop, psi,
  * field coefficients c1[i] / c2[i] and stream streams[i]; grids, degrees and
  * physics may differ) advanced by one step h each, concurrently. Host threads
@@ -301,9 +318,39 @@ tdz_status tdz_prop_step(tdz_prop *p, void *psi, double h, const double *c1, con
 tdz_status tdz_prop_step_batch(int count, tdz_prop *const *props, void *const *psis, double h,
                                const double *const *c1, const double *const *c2, void *const *streams, int threads);
 
+/* Totals: stage solves, Krylov iterations, FP64 operator applies of the
+ * solver, multigrid cycles; last solve's iterations and relative residual. */
 tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies,
                           long long *cycles, int *last_its, double *last_rres);
+/* Preconditioner rebuilds the refresh rule asked for (tdz_pc_refresh_stale
+ * over the stage solves of this propagator). */
+tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds);
 void tdz_prop_destroy(tdz_prop *p);
+
+/* Preconditioner refresh rule of TDSEZPCRefresh::Stale
+ * (include/tdsez_propagator.hpp:17-31): the preconditioner built from one
+ * stage is reused; the first solve after a build sets base, and a solve
+ * needing more than 2 base + 5 iterations, or more than cap when cap >= 0
+ * (-tdsez_pc_refresh_its), asks for a rebuild. Start from
+ * {base = -1, rebuilds = 0, cap}. Host only. */
+typedef struct tdz_pc_refresh {
+    int base;
+    int rebuilds;
+    int cap;
+} tdz_pc_refresh;
+/* Record a solve of `its` iterations; returns 1 when the preconditioner
+ * should be rebuilt before the next solve, else 0. */
+int tdz_pc_refresh_stale(tdz_pc_refresh *r, int its);
+
+/* Strong-field check of TDSEZSetupMultigrid (src/multigrid.cpp:213-237):
+ * *ratio = tau max_t sum_a |E_a(t)| L_a over 4 T / dt + 1 samples of [0, T],
+ * with L_a = max(|lo_a|, |hi_a|) of the space's box and tau the stage scale
+ * of the propagator kind (CN dt/2, Pade(2,2) dt/sqrt12, Magnus-4
+ * dt/(2 sqrt12)); field(a, t, ctx) returns the physical field. Above 1.5 the
+ * field term dominates the stage operator and multigrid may not converge
+ * (the reference warns; the host layer here does the same). Host only. */
+tdz_status tdz_strong_field_ratio(const tdz_space *s, int kind, double dt, double final_time, tdz_field_fn field,
+                                  void *ctx, double *ratio);
 
 /* --------------------------------------------------------------- t-SURFF
  * Photoelectron amplitudes from the surface flux through the box |x_d| = R
@@ -315,7 +362,6 @@ void tdz_prop_destroy(tdz_prop *p);
  * ordered k_x slowest, k_z fastest. The field callback returns the physical
  * field E_a(t) (0 on uncoupled axes).
  */
-typedef double (*tdz_field_fn)(int axis, double t, void *ctx);
 typedef struct tdz_tsurff tdz_tsurff;
 typedef struct tdz_tsurff_opts {
     double radius;      /* SurffRadius R                                     */

@@ -128,3 +128,42 @@ def ground_state(asm: Assembled, target: float = 0.0, k: int = 1):
 
 def expect(A, psi):
     return np.vdot(psi, A @ psi)
+
+
+class PCRefreshRule:
+    """The preconditioner refresh rule of ``TDSEZPCRefresh::Stale``
+    (``include/tdsez_propagator.hpp:17-31``): the first solve after a build
+    sets the base; a solve with more than 2 base + 5 iterations, or more than
+    ``cap`` when cap >= 0 (``-tdsez_pc_refresh_its``), asks for a rebuild."""
+
+    def __init__(self, cap: int = -1):
+        self.base, self.rebuilds, self.cap = -1, 0, cap
+
+    def stale(self, its: int) -> bool:
+        if self.cap >= 0 and its > self.cap:
+            self.base = -1
+            self.rebuilds += 1
+            return True
+        if self.base < 0:
+            self.base = its
+            return False
+        if its <= 2 * self.base + 5:
+            return False
+        self.base = -1
+        self.rebuilds += 1
+        return True
+
+
+def strong_field_ratio(kind: str, dt: float, final_time: float, field, bounds) -> float:
+    """tau max_t sum_a |E_a(t)| L_a of ``TDSEZSetupMultigrid``'s strong-field
+    check (``src/multigrid.cpp:213-237``): 4 T/dt + 1 equispaced samples of
+    [0, T], L_a = max(|lo_a|, |hi_a|), tau = dt/2 (CN), dt/sqrt12 (Pade(2,2)),
+    dt/(2 sqrt12) (Magnus-4). ``field(a, t)`` is the physical field."""
+    tau = {"cn": 0.5 * dt, "pade22": dt / math.sqrt(12.0), "magnus4": dt / (2.0 * math.sqrt(12.0))}[kind]
+    L = [max(abs(lo), abs(hi)) for lo, hi in bounds]
+    n = int(math.ceil(4.0 * final_time / dt))
+    worst = 0.0
+    for i in range(n + 1):
+        t = final_time * i / max(n, 1)
+        worst = max(worst, sum(abs(field(a, t)) * L[a] for a in range(len(L))))
+    return tau * worst

@@ -54,7 +54,12 @@ class tdz_solver_opts(C.Structure):
         ("outer_precision", C.c_int),
         ("mg_learned", C.c_int),
         ("relaxed", C.c_int),
+        ("pc_refresh_its", C.c_int),
     ]
+
+
+class tdz_pc_refresh(C.Structure):
+    _fields_ = [("base", C.c_int), ("rebuilds", C.c_int), ("cap", C.c_int)]
 
 
 class tdz_tsurff_opts(C.Structure):
@@ -121,6 +126,10 @@ SIGNATURES = {
     "tdz_solver_train_coarse": (I, [VP, I, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), VP]),
     "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
     "tdz_set_autotune": (None, [I]),
+    "tdz_set_apply3d_shape": (None, [I, I]),
+    "tdz_prop_refreshes": (I, [VP, C.POINTER(LL)]),
+    "tdz_pc_refresh_stale": (I, [C.POINTER(tdz_pc_refresh), I]),
+    "tdz_strong_field_ratio": (I, [VP, I, D, D, FIELD_FN, VP, C.POINTER(D)]),
     "tdz_prop_step_batch": (I, [I, C.POINTER(VP), C.POINTER(VP), C.c_double, C.POINTER(C.POINTER(C.c_double)),
                                 C.POINTER(C.POINTER(C.c_double)), C.POINTER(VP), I]),
     "tdz_observables": (I, [VP, VP, C.POINTER(C.c_double), VP]),

@@ -43,6 +43,20 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 static std::atomic<long long> g_launches{0};
 void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+int sm_count() {
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    int dev = 0;
+    TDZ_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    TDZ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    n = std::max(1, n);
+    cache[dev] = n;
+    return n;
+}
 }  // namespace tdz
 
 template <class F> static tdz_status guarded(F &&f) {
@@ -184,9 +198,24 @@ long long tdz_operator_launches(const tdz_op *op) { return op ? op->o.launches :
 void tdz_operator_destroy(tdz_op *op) { delete op; }
 
 namespace {
-// per-device reduction scratch of tdz_vec_dot (allocated on first use)
+// Reduction scratch of tdz_vec_dot / tdz_vec_mdot, one per (device, stream),
+// allocated and initialised on first use under the lock: calls on different
+// streams never share partial sums, calls on one stream are ordered by it.
 std::mutex g_dot_mu;
-std::map<int, std::unique_ptr<tdz::blas::Reducer>> g_dot_scratch;
+std::map<std::pair<int, cudaStream_t>, std::unique_ptr<tdz::blas::Reducer>> g_dot_scratch;
+
+tdz::blas::Reducer *dot_scratch(cudaStream_t st) {
+    int dev = 0;
+    TDZ_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_dot_mu);
+    auto &slot = g_dot_scratch[{dev, st}];
+    if (!slot) {
+        auto r = std::make_unique<tdz::blas::Reducer>();
+        r->init();
+        slot = std::move(r);
+    }
+    return slot.get();
+}
 }  // namespace
 
 tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision, void *out, void *stream) {
@@ -194,17 +223,9 @@ tdz_status tdz_vec_dot(const void *x, const void *y, long long n, int precision,
         TDZ_CHECK(x && y && out, TDZ_ERR_ARG, "null argument");
         TDZ_CHECK(n >= 0, TDZ_ERR_ARG, "negative length");
         TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
-        int dev = 0;
-        TDZ_CUDA(cudaGetDevice(&dev));
-        tdz::blas::Reducer *r;
-        {
-            std::lock_guard<std::mutex> lk(g_dot_mu);
-            auto &slot = g_dot_scratch[dev];
-            if (!slot) slot = std::make_unique<tdz::blas::Reducer>();
-            r = slot.get();
-        }
-        tdz::blas::dot_device(*r, x, y, (size_t)n, precision, static_cast<double2 *>(out),
-                              static_cast<cudaStream_t>(stream));
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        tdz::blas::Reducer *r = dot_scratch(st);
+        tdz::blas::dot_device(*r, x, y, (size_t)n, precision, static_cast<double2 *>(out), st);
     });
 }
 
@@ -215,17 +236,8 @@ tdz_status tdz_vec_mdot(const void *const *V, int k, const void *w, long long n,
         TDZ_CHECK(k >= 1 && n >= 0, TDZ_ERR_ARG, "bad sizes");
         TDZ_CHECK(precision == TDZ_FP32 || precision == TDZ_FP64, TDZ_ERR_ARG, "bad precision");
         for (int i = 0; i < k; ++i) TDZ_CHECK(V[i], TDZ_ERR_ARG, "null vector in V");
-        int dev = 0;
-        TDZ_CUDA(cudaGetDevice(&dev));
-        tdz::blas::Reducer *r;
-        {
-            std::lock_guard<std::mutex> lk(g_dot_mu);
-            auto &slot = g_dot_scratch[dev];
-            if (!slot) slot = std::make_unique<tdz::blas::Reducer>();
-            r = slot.get();
-        }
-        r->init();
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        tdz::blas::Reducer *r = dot_scratch(st);
         double2 *o = static_cast<double2 *>(out);
         for (int c0 = 0; c0 < k; c0 += tdz::blas::kMaxDot) {
             const int kk = std::min(tdz::blas::kMaxDot, k - c0);
@@ -260,6 +272,7 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     so.outer = o->outer_precision == 0 ? TDZ_FP64 : o->outer_precision;
     so.mg.learned = o->mg_learned;
     so.relaxed = o->relaxed != 0;
+    so.pc_refresh_its = o->pc_refresh_its > 0 ? o->pc_refresh_its : -1;
     TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
               "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;
@@ -280,6 +293,8 @@ tdz_status tdz_plane_transform(const double *B, int K, int N, const float *in, i
 }
 
 void tdz_set_autotune(int on) { tdz::set_autotune(on); }
+
+void tdz_set_apply3d_shape(int tile_x, int run) { tdz::set_forced_shape(tile_x, run); }
 
 tdz_status tdz_observables(tdz_op *op, const void *psi, double *out, void *stream) {
     return guarded([&] {
@@ -444,7 +459,51 @@ tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, 
     });
 }
 
+tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds) {
+    return guarded([&] {
+        TDZ_CHECK(p && rebuilds, TDZ_ERR_ARG, "null argument");
+        *rebuilds = (long long)p->p.refresh[0].rebuilds + p->p.refresh[1].rebuilds;
+    });
+}
+
 void tdz_prop_destroy(tdz_prop *p) { delete p; }
+
+int tdz_pc_refresh_stale(tdz_pc_refresh *r, int its) {
+    if (!r) return 0;
+    tdz::PCRefresh f;
+    f.base = r->base;
+    f.rebuilds = r->rebuilds;
+    f.cap = r->cap;
+    const bool stale = f.stale(its);
+    r->base = f.base;
+    r->rebuilds = f.rebuilds;
+    return stale ? 1 : 0;
+}
+
+tdz_status tdz_strong_field_ratio(const tdz_space *s, int kind, double dt, double final_time, tdz_field_fn field,
+                                  void *ctx, double *ratio) {
+    return guarded([&] {
+        TDZ_CHECK(s && field && ratio, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(dt > 0.0 && final_time >= 0.0, TDZ_ERR_ARG, "dt must be positive, final_time non-negative");
+        TDZ_CHECK(kind >= 0 && kind <= 2, TDZ_ERR_ARG, "unknown propagator kind");
+        const double s12 = std::sqrt(12.0);
+        const double tau = kind == TDZ_CN ? 0.5 * dt : (kind == TDZ_PADE22 ? dt / s12 : dt / (2.0 * s12));
+        double L[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < s->s.dim; ++a) {
+            const auto &U = s->s.ax[a].U;
+            L[a] = std::max(std::abs(U.front()), std::abs(U.back()));
+        }
+        const long long n = (long long)std::ceil(4.0 * final_time / dt);
+        double worst = 0.0;
+        for (long long i = 0; i <= n; ++i) {
+            const double t = final_time * (double)i / (double)std::max<long long>(n, 1);
+            double v = 0.0;
+            for (int a = 0; a < s->s.dim; ++a) v += std::abs(field(a, t, ctx)) * L[a];
+            worst = std::max(worst, v);
+        }
+        *ratio = tau * worst;
+    });
+}
 
 tdz_status tdz_tsurff_create(const tdz_space *s, const tdz_tsurff_opts *o, tdz_field_fn field, void *ctx,
                              tdz_tsurff **out) {

@@ -18,14 +18,27 @@ std::map<TuneKey, std::pair<int, int>> g_tune;
 }  // namespace
 
 bool autotune_enabled() { return g_autotune.load() != 0; }
-bool forced_shape(int *txw, int *run) {
-    static const char *v = std::getenv("TDZ_APPLY3D_SHAPE");
-    if (!v) return false;
+namespace {
+// forced launch shape of the 3D apply, packed (tile_x << 32 | run); 0 = none.
+// Initialised from TDZ_APPLY3D_SHAPE="tile_x,run", changed by tdz_set_apply3d_shape.
+long long shape_from_env() {
+    const char *v = std::getenv("TDZ_APPLY3D_SHAPE");
     int a = 0, b = 0;
-    if (std::sscanf(v, "%d,%d", &a, &b) != 2 || a <= 0 || b <= 0) return false;
-    *txw = a;
-    *run = b;
+    if (!v || std::sscanf(v, "%d,%d", &a, &b) != 2 || a <= 0 || b <= 0) return 0;
+    return ((long long)a << 32) | (unsigned)b;
+}
+std::atomic<long long> g_shape{shape_from_env()};
+}  // namespace
+
+bool forced_shape(int *txw, int *run) {
+    const long long v = g_shape.load();
+    if (!v) return false;
+    *txw = (int)(v >> 32);
+    *run = (int)(v & 0xffffffffLL);
     return true;
+}
+void set_forced_shape(int txw, int run) {
+    g_shape.store(txw > 0 && run > 0 ? (((long long)txw << 32) | (unsigned)run) : 0);
 }
 bool tune_verbose() {
     static const bool v = std::getenv("TDZ_AUTOTUNE_VERBOSE") != nullptr;

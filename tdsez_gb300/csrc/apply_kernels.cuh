@@ -499,9 +499,10 @@ template <class T, bool HB, bool HC> struct TileY {
     static constexpr int v = std::is_same<T, float>::value || (HB && HC) ? 8 : 16;
 };
 
-// z chunk per CTA: about `target` CTAs in total, chunks no shorter than 4p
-// planes (the 2p halo planes of a chunk are re-read)
-inline int pick_chunk(int tiles, int n_outer, int P, int target = 152 * 8) {
+// z chunk per CTA: about `target` CTAs in total (0: 8 per SM), chunks no
+// shorter than 4p planes (the 2p halo planes of a chunk are re-read)
+inline int pick_chunk(int tiles, int n_outer, int P, int target = 0) {
+    if (target <= 0) target = 8 * sm_count();
     int chunks = (target + tiles - 1) / tiles;
     chunks = std::max(1, std::min(chunks, n_outer / std::max(1, 4 * P)));
     return (n_outer + chunks - 1) / chunks;
@@ -535,8 +536,10 @@ struct TuneKey {
 };
 bool autotune_enabled();
 bool tune_verbose();   // TDZ_AUTOTUNE_VERBOSE set: the autotuner prints each candidate's time
-// TDZ_APPLY3D_SHAPE="tile_x,run": a fixed launch shape for every 3D apply (no autotuning)
+// a fixed launch shape for every 3D apply (no autotuning): TDZ_APPLY3D_SHAPE="tile_x,run"
+// in the environment at load time, or tdz_set_apply3d_shape
 bool forced_shape(int *txw, int *run);
+void set_forced_shape(int txw, int run);
 bool tune_lookup(const TuneKey &k, int *txw, int *zchunk);
 void tune_store(const TuneKey &k, int txw, int zchunk);
 

@@ -17,11 +17,12 @@ namespace blas {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRedBlocks = 8 * 152;   // about 8 CTAs per SM: latency hiding for the double-float dots
+// about 8 CTAs per SM: latency hiding for the double-float dots
+inline int red_blocks() { return 8 * sm_count(); }
 
 inline int grid_for(size_t n) {
     const size_t b = (n + kThreads - 1) / kThreads;
-    return (int)std::min<size_t>(std::max<size_t>(b, 1), 8 * 152);
+    return (int)std::min<size_t>(std::max<size_t>(b, 1), (size_t)red_blocks());
 }
 
 template <class C> __device__ __forceinline__ C cmk(double re, double im) {
@@ -431,10 +432,11 @@ void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
 
 void Reducer::init() {
     if (blocks) return;
-    blocks = kRedBlocks;
-    partial.alloc(sizeof(double2) * (kMaxDot + 1) * blocks);
+    const int nb = red_blocks();
+    partial.alloc(sizeof(double2) * (kMaxDot + 1) * nb);
     result.alloc(sizeof(double2) * (kMaxDot + 1));
-    TDZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host), sizeof(double2) * (kMaxDot + 1)));
+    if (!host) TDZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host), sizeof(double2) * (kMaxDot + 1)));
+    blocks = nb;   // last: a Reducer with blocks != 0 has all its buffers
 }
 
 Reducer::~Reducer() {
@@ -540,7 +542,7 @@ void gs_update(Reducer &r, void *w, int k, const void *const *V, const cd *a, si
 }
 
 void cn_combine(void *psi, const void *x, const void *z, cd c, size_t n, cudaStream_t st) {
-    const int g = (int)std::min<size_t>((n + kThreads - 1) / kThreads, (size_t)kRedBlocks);
+    const int g = (int)std::min<size_t>((n + kThreads - 1) / kThreads, (size_t)red_blocks());
     k_cn_combine<<<g, kThreads, 0, st>>>(static_cast<double2 *>(psi), static_cast<const double2 *>(x),
                                          static_cast<const double2 *>(z), cdf_host(c), n);
     TDZ_CUDA(cudaGetLastError());

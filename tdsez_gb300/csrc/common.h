@@ -30,6 +30,10 @@ void set_last_error(const std::string &msg);
 void count_launch(long long n = 1);
 long long launch_count();
 
+// Multiprocessors of the current device (looked up once per device; grids
+// of the persistent and grid-stride kernels are sized in multiples of it).
+int sm_count();
+
 #define TDZ_CHECK(cond, code, msg)                                                          \
     do {                                                                                    \
         if (!(cond)) throw ::tdz::Error((code), std::string(msg) + " (" __FILE__ ":" +      \

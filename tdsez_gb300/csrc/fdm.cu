@@ -930,7 +930,7 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
     if (tensor) {
         // [z][y][c][x] -> [z][x'][c][y] -> [z][y'][c][x'] -> line solves -> [z][x][c][y'] -> [z][y][c][x]
         float *a = pa.as<float>(), *b = pb.as<float>();
-        const int blocks = (int)std::min<size_t>((N + 255) / 256, 152 * 16);
+        const int blocks = (int)std::min<size_t>((N + 255) / 256, (size_t)16 * sm_count());
         k_to_planar<<<blocks, 256, 0, st>>>(r, a, n[0], rows, ldx);
         transform(Tf[0], a, n[2], n[1], ldx, b, ldy, st);
         transform(Tf[1], b, n[2], n[0], ldy, a, ldx, st);

@@ -50,7 +50,7 @@ void axis_contract(const RowSparse &A, int axis, const void *in, void *out, int 
     o[axis] = A.rows;
     const size_t total = (size_t)o[0] * o[1] * o[2];
     const int threads = 256;
-    const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, 16 * 152);
+    const int blocks = (int)std::min<size_t>((total + threads - 1) / threads, (size_t)16 * sm_count());
     if (prec == TDZ_FP64)
         k_axis_contract<double><<<blocks, threads, 0, st>>>(A.dcol.as<int>(), A.dval64.as<double>(), A.width, axis,
                                                             static_cast<const double2 *>(in), static_cast<double2 *>(out),

@@ -94,6 +94,8 @@ enum BaseId { kM = 0, kS = 1, kX = 2 };
 
 // launch-shape autotuning of the 3D apply (apply.cu; on by default)
 void set_autotune(int on);
+// fixed launch shape of every fused 3D apply (tile_x, run; 0 = autotune), apply.cu
+void set_forced_shape(int txw, int run);
 
 // kernel launchers (apply.cu)
 // Extras of one apply, fused into its store: y = sub - op x when sub is

@@ -96,7 +96,11 @@ void Propagator::setup(Operator *op_, int kind_, const SolverOptions &o, int gue
     // (src/propagator.cpp:446-460); the multigrid follows later stage changes
     nsolvers = kind == 0 ? 1 : 2;
     aprec = o.outer;
-    for (int k = 0; k < nsolvers; ++k) solver[k].setup(op, o, st);
+    for (int k = 0; k < nsolvers; ++k) {
+        solver[k].setup(op, o, st);
+        refresh[k] = PCRefresh{};
+        refresh[k].cap = o.pc_refresh_its;
+    }
 }
 
 void Propagator::extrapolate(int slot, double2 *psi, cudaStream_t st) {

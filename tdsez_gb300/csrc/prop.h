@@ -18,6 +18,7 @@ struct SolverOptions {
     int pc_precision = TDZ_FP32;
     int outer = TDZ_FP64;  // operator applies of FGMRES and the right-hand sides (TDZ_FP64 or TDZ_FP64_DF)
     bool relaxed = false;  // FP32 Arnoldi applies, true residual in `outer` at every restart
+    int pc_refresh_its = -1;   // propagators: rebuild the preconditioner above this many iterations (-1: off)
     MGOptions mg;
 };
 

@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <set>
 
 namespace tdz {
 
@@ -354,16 +355,6 @@ float tf32_round_host(double v) {
     return f;
 }
 
-int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        TDZ_CUDA(cudaGetDevice(&dev));
-        TDZ_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-    }
-    return n;
-}
-
 // 256-row tiles where two sub-tiles' stages fit in shared memory (Np <= 192), else 128
 template <int NP> constexpr int sub_tiles() { return TGShape<NP, 2>::fits ? 2 : 1; }
 
@@ -371,10 +362,18 @@ template <int NP>
 void launch(const TransformMat &T, const float *in, int ldi, TGParams prm, cudaStream_t st) {
     constexpr int MS = sub_tiles<NP>();
     const size_t smem = TGShape<NP, MS>::SMEM;
-    static bool attr = false;   // set once per process (same device attribute for every device)
-    if (!attr) {
-        TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
+    // opt-in to the tile's shared memory once per device (guarded: the batch
+    // API steps runs from several host threads)
+    {
+        static std::mutex mu;
+        static std::set<int> done;
+        int dev = 0;
+        TDZ_CUDA(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> lk(mu);
+        if (!done.count(dev)) {
+            TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            done.insert(dev);
+        }
     }
     CUtensorMap amap;
     make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)(TM * MS));

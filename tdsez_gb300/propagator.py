@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import warnings
 from typing import Callable, Optional, Sequence
 
 from . import _lib
@@ -25,11 +26,13 @@ MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 
 def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
                 maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 0, mg_coarse_its: int = 12,
-                outer: str = "fp64", mg_learned: bool = False, relaxed: bool = False):
+                outer: str = "fp64", mg_learned: bool = False, relaxed: bool = False, pc_refresh_its: int = 0):
     """Solver options. ``precision`` is the preconditioner's arithmetic
     (fp32 = mixed precision); ``outer`` the arithmetic of the FP64 Krylov
     method's operator applies: "fp64" (native) or "df" (double-float on the
-    FP32 pipes, about 48 significant bits)."""
+    FP32 pipes, about 48 significant bits). ``pc_refresh_its`` > 0 also
+    rebuilds a propagator's preconditioner whenever a stage solve takes more
+    iterations (-tdsez_pc_refresh_its)."""
     o = _lib.tdz_solver_opts()
     o.restart = restart
     o.maxit = maxit
@@ -42,6 +45,7 @@ def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, re
     o.outer_precision = {"fp64": _lib.TDZ_FP64, "df": _lib.TDZ_FP64_DF}[outer]
     o.mg_learned = 1 if mg_learned else 0
     o.relaxed = 1 if relaxed else 0
+    o.pc_refresh_its = max(0, int(pc_refresh_its))
     return o
 
 
@@ -141,10 +145,34 @@ class Propagator:
                                              C.c_void_p(_stream(stream))))
         return psi
 
+    def strong_field_ratio(self, dt: float, final_time: float) -> float:
+        """tau max_t sum_a |E_a(t)| L_a over the run (the strong-field check
+        of TDSEZSetupMultigrid, src/multigrid.cpp:213-237)."""
+        coupled = list(self.op.coupled)
+
+        def fn(axis, t, ctx):
+            if axis not in coupled:
+                return 0.0
+            return float(self.field(t)[coupled.index(axis)])
+        cb = _lib.FIELD_FN(fn)
+        out = C.c_double()
+        _lib.check(_lib.load().tdz_strong_field_ratio(self.op.space.handle, KINDS[self.kind], dt, final_time, cb,
+                                                      None, C.byref(out)))
+        return out.value
+
     def evolve(self, psi, dt: float, final_time: float, monitor=None, stream=None):
         """Steps t_k = k dt, the last one shortened to end at final_time
         (``src/propagator.cpp:734-741``); ``monitor(step, t, psi)`` after
-        every step and at t = 0."""
+        every step and at t = 0. With the multigrid preconditioner a field
+        that dominates the stage operator (tau max|E.r| > 1.5) is warned
+        about first, as the reference does."""
+        if self.opts.pc == PCS["mg"] and not getattr(self, "_field_checked", False):
+            self._field_checked = True
+            r = self.strong_field_ratio(dt, final_time)
+            if r > 1.5:
+                warnings.warn("tau*max|E.r| = %.2g > 1.5: the field term dominates the propagator operator and "
+                              "multigrid may not converge; use the FDM or mass preconditioner or a smaller "
+                              "time step" % r, RuntimeWarning, stacklevel=2)
         n = int(math.ceil(final_time / dt - 1e-9))
         if monitor:
             monitor(0, 0.0, psi)
@@ -165,6 +193,12 @@ class Propagator:
                                               C.byref(li), C.byref(rr)))
         return {"solves": s.value, "its": i.value, "applies": a.value, "cycles": cy.value,
                 "last_its": li.value, "last_rres": rr.value}
+
+    def refreshes(self) -> int:
+        """Preconditioner rebuilds the refresh rule asked for so far."""
+        n = C.c_longlong()
+        _lib.check(_lib.load().tdz_prop_refreshes(self.handle, C.byref(n)))
+        return n.value
 
     def __del__(self):
         h = getattr(self, "handle", None)

@@ -148,6 +148,13 @@ def _soft_value(soft, r):
 
 def oracle_of(c):
     """Oracle Space, Physics, Assembled for a case dict."""
+    S, ph = oracle_space_phys(c)
+    return S, ph, oo.Assembled(S, ph)
+
+
+def oracle_space_phys(c):
+    """Oracle Space and Physics for a case dict, without assembling (large
+    separable cases use the oracle's Kronecker apply instead)."""
     axes = [ob.Axis(k, c["p"], c["nq"]) for k in c["knots"]]
     S = ob.Space(axes)
     dim = S.dim
@@ -176,7 +183,17 @@ def oracle_of(c):
                         mass_const=None, mass_axis=ma, pot_separable=[Vs[d] for d in range(dim)],
                         cap_kmin=c.get("cap_kmin"), bounds=c.get("bounds", ()), coupled=c["coupled"],
                         dirichlet=c.get("dirichlet", False))
-    return S, ph, oo.Assembled(S, ph)
+    return S, ph
+
+
+def workload_case(nel, p=3):
+    """The benchmark's 3D heterostructure (tdsez_gb300.workloads) at another
+    element count, as a case dict: same box, layers, masses, potentials and
+    field axis."""
+    from tdsez_gb300.workloads import heterostructure
+    w = heterostructure(nel=nel, p=p)
+    return dict(knots=w.knots, p=w.p, nq=w.nq, charge=w.phys.charge, mass_axis=2, inv_mass=w.phys.inv_mass_fn,
+                V=list(w.phys.potential), coupled=(2,)), w
 
 
 def product_of(c):

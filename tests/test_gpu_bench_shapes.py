@@ -1,0 +1,115 @@
+"""GPU parity at the benchmark's launch shapes: the 3D heterostructure of the
+CN steps/s workload (same box, layers, masses, potential and field axis) at
+136 x 24 x 96 elements (N = 139 x 27 x 109 = 409 077), checked against the
+oracle's FP64 Kronecker apply (itself pinned to the assembled operators).
+
+At this size the paths that the small parity cases never reach all run:
+tile widths 16..32 with several tiles along x and y, persistent CTAs whose
+run of (tile, z) planes crosses from one tile into the next (runs of 133
+planes over z columns of 109), the fused residual / norm / dot reductions
+of the FGMRES applies, the tensor-core eigenvector transform with N = 139 >
+128 (the 144-column variant), and the two-thread line solve along z.
+Bars: stage and mass applies 1e-12 (FP64 and double-float) and 1e-6 (FP32),
+max-norm relative; one CN step's stage system solved to a true relative
+residual <= 1e-10 (1.5e-10 allowed for the FP64 re-evaluation)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from oracle import operators as oo
+from tests.cases import oracle_space_phys, product_of, workload_case
+
+NEL = (136, 24, 96)
+# None: the autotuned shape; (16, 133): the shape the tuner picks on the
+# 160 x 160 x 320 workload for the double-float stage apply
+SHAPES = [None, (16, 133), (16, 20), (28, 64), (32, 300)]
+TOL = {"fp64": 1e-12, "df": 1e-12, "fp32": 1e-6}
+
+
+@pytest.fixture(scope="module")
+def mid(cuda):
+    c, w = workload_case(NEL)
+    S, ph = oracle_space_phys(c)
+    PS, op = product_of(c)
+    assert PS.ndof == S.ndof == 139 * 27 * 109
+    return dict(c=c, w=w, S=S, ph=ph, op=op)
+
+
+def _shape(shape):
+    from tdsez_gb300 import _lib
+    lib = _lib.load()
+    if shape is None:
+        lib.tdz_set_apply3d_shape(0, 0)
+    else:
+        lib.tdz_set_apply3d_shape(*shape)
+
+
+def _rel(y, ref):
+    return np.abs(y - ref).max() / np.abs(ref).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", SHAPES)
+def test_stage_and_mass_apply_at_bench_shapes(mid, shape):
+    import torch
+    from tdsez_gb300 import _lib
+    S, ph, op = mid["S"], mid["ph"], mid["op"]
+    rng = np.random.default_rng(17)
+    x = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    s3 = math.sqrt(3.0)
+    stages = [(1.0, 0.25j, [0.004]),                              # CN, dt = 0.5
+              (1.0, 0.5 * (-s3 + 3j) / 12.0, [-0.002 + 0.001j])]   # Pade(2,2) first stage
+    try:
+        _shape(shape)
+        for alpha, g, cc in stages:
+            op.set_stage(alpha, g, cc)
+            ref_a = oo.kron_apply(S, oo.kron_terms(S, ph, g=g, c=cc, alpha=alpha), x)
+            ref_m = oo.kron_apply(S, oo.kron_terms(S, ph, g=0.0, alpha=1.0)[:1], x)
+            for prec, dt in (("fp64", torch.complex128), ("df", torch.complex128), ("fp32", torch.complex64)):
+                xd = torch.tensor(x, dtype=dt, device="cuda")
+                for which, ref in ((_lib.TDZ_STAGE, ref_a), (_lib.TDZ_MASS, ref_m)):
+                    yd = torch.full_like(xd, float("nan"))
+                    op.apply(which, xd, yd, df=prec == "df")
+                    torch.cuda.synchronize()
+                    err = _rel(yd.cpu().numpy().astype(np.complex128), ref)
+                    assert err < TOL[prec], (shape, g, prec, which, err)
+    finally:
+        _shape(None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [None, (16, 133)])
+def test_cn_step_at_bench_shapes(mid, shape):
+    """One CN step exactly as the bench runs it (FP32 fast-diagonalisation
+    preconditioner, double-float FGMRES applies with the fused residual,
+    norm and dot reductions, x0 = P^-1 b, the fused CN update), then the
+    stage system re-evaluated by the oracle in FP64."""
+    import torch
+    from tdsez_gb300.propagator import Propagator
+    S, ph, op, w = mid["S"], mid["ph"], mid["op"], mid["w"]
+    try:
+        _shape(shape)
+        psi0 = op.separable_state(w.packet)
+        # a packet with structure on every axis, not only the smooth ground-state-like one
+        rng = np.random.default_rng(23)
+        noise = torch.tensor(1e-3 * (rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)), device="cuda")
+        psi0 = psi0 + noise
+        G = Propagator(op, "cn", field=w.field, pc="fdm", precision="fp32", rtol=1e-10, outer="df", guess_order=-1)
+        t, dt = 200.0, w.dt
+        psi = psi0.clone()
+        G.step(psi, t, dt)
+        torch.cuda.synchronize()
+        st = G.stats()
+        p0, p1 = psi0.cpu().numpy(), psi.cpu().numpy()
+        X = 0.5 * (p0 + p1)
+        cc = [ph.sign * e for e in w.field(t + 0.5 * dt)]
+        b = oo.kron_apply(S, oo.kron_terms(S, ph, g=0.0, alpha=1.0)[:1], p0)
+        AX = oo.kron_apply(S, oo.kron_terms(S, ph, g=0.5j * dt, c=cc, alpha=1.0), X)
+        rres = np.linalg.norm(b - AX) / np.linalg.norm(b)
+        assert st["last_rres"] <= 1e-10, st
+        assert rres <= 1.5e-10, (shape, rres, st)
+        assert st["its"] <= 2, st
+    finally:
+        _shape(None)
