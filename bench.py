@@ -492,7 +492,7 @@ def main():
     ap.add_argument("--outer", default="df", choices=["df", "fp64"])
     ap.add_argument("--guess-order", type=int, default=-1)
     ap.add_argument("--rtol", type=float, default=RTOL)
-    ap.add_argument("--relaxed", default="off", choices=["on", "off"])
+    ap.add_argument("--relaxed", default="on", choices=["on", "off"])
     ap.add_argument("--apply-only", action="store_true")
     ap.add_argument("--precond-only", action="store_true")
     ap.add_argument("--batch-scan", type=int, default=0, help="runs of the batched 2D scan (0: headline bench)")

@@ -37,6 +37,12 @@ typedef int tdz_status;
  * relative error near 1e-14, several times the speed of native FP64 on
  * GB300. Accepted by tdz_operator_apply and as tdz_solver_opts.outer_precision. */
 #define TDZ_FP64_DF 2
+/* FP64 vectors whose operator apply computes in FP32 arithmetic (inputs
+ * truncated to 24 bits, results widened exactly): the FP32 apply's accuracy
+ * at FP64 storage, for corrections whose own size bounds the error (relaxed
+ * Krylov steps). 3D operators without the soft-core quadrature term;
+ * accepted by tdz_operator_apply. */
+#define TDZ_FP64_F32 3
 
 /* operators selectable in tdz_operator_apply */
 #define TDZ_MASS 0        /* M  = int B_i B_j                                  */
@@ -129,7 +135,8 @@ tdz_status tdz_operator_set_stage(tdz_op *op, double alpha_re, double alpha_im, 
 /* y = op x. Replaces MatMult on M, H, D_a and the stage matrices
  * (src/propagator.cpp:622-623, src/monitor.cpp:114-116) and
  * TDSEZTensorOps::Apply (src/tensorops.cpp:155-188). x and y must not alias.
- * precision: TDZ_FP32, TDZ_FP64 or TDZ_FP64_DF (FP64 vectors). */
+ * precision: TDZ_FP32, TDZ_FP64, or TDZ_FP64_DF / TDZ_FP64_F32 (FP64 vectors);
+ * FP64 vectors must be 16-byte aligned. */
 tdz_status tdz_operator_apply(tdz_op *op, int which, int precision, const void *x, void *y, void *stream);
 /* x <- M^-1 x in place (exact Kronecker inverse of the overlap, banded
  * Cholesky line solves), FP32 or FP64 device vector. */
@@ -195,7 +202,7 @@ typedef struct tdz_solver_opts {
                            A z_j in FP32, the residual b - A x of every
                            restart in outer_precision. A cycle that reports
                            convergence is accepted when the estimate plus
-                           the bound sum_j |y_j| 1e-4 ||A z_j|| on its gap
+                           the bound sum_j |y_j| gamma |||A||| ||z_j|| on its gap
                            to the true residual meets rtol (rnorm returns
                            that sum), else one more restart residual
                            decides                                           */

@@ -12,7 +12,7 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "libtdz.so"
 
 TDZ_OK = 0
-TDZ_FP32, TDZ_FP64, TDZ_FP64_DF = 0, 1, 2
+TDZ_FP32, TDZ_FP64, TDZ_FP64_DF, TDZ_FP64_F32 = 0, 1, 2, 3
 TDZ_MASS, TDZ_HAMILTONIAN, TDZ_DIPOLE_X, TDZ_DIPOLE_Y, TDZ_DIPOLE_Z, TDZ_STAGE = range(6)
 
 STATUS_NAMES = {0: "TDZ_OK", 1: "TDZ_ERR_ARG", 2: "TDZ_ERR_CUDA", 3: "TDZ_ERR_NOT_CONVERGED",

@@ -1,8 +1,9 @@
 // Dispatch of the fused apply: stage scalars folded into the kernel
 // parameters, degree-specific instantiations in apply_p<P>.cu.
-#include "apply_kernels.cuh"
+#include "apply3d_rb.cuh"
 
 #include <atomic>
+#include <cstring>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -45,6 +46,59 @@ bool tune_verbose() {
     return v;
 }
 void set_autotune(int on) { g_autotune.store(on ? 1 : 0); }
+
+// error word of the 3D apply kernels' bounded waits, one per device,
+// allocated with the first apply on the device
+int *apply_error_word() {
+    static std::mutex mu;
+    static std::map<int, int *> words;
+    int dev = 0;
+    TDZ_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = words.find(dev);
+    if (it != words.end()) return it->second;
+    int *p = nullptr;
+    TDZ_CUDA(cudaMalloc(&p, sizeof(int)));
+    TDZ_CUDA(cudaMemset(p, 0, sizeof(int)));
+    words[dev] = p;
+    return p;
+}
+
+int take_apply_error() {
+    int *p = apply_error_word();
+    int v = 0;
+    TDZ_CUDA(cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) TDZ_CUDA(cudaMemset(p, 0, sizeof(int)));
+    return v;
+}
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 rb_encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    TDZ_CHECK(fn != nullptr, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+}  // namespace
+
+void rb_make_map(CUtensorMap *map, const void *x, int n0, int n1, int n2, int boxx, int boxy) {
+    const cuuint64_t dims[3] = {(cuuint64_t)2 * n0, (cuuint64_t)n1, (cuuint64_t)n2};
+    const cuuint64_t strides[2] = {(cuuint64_t)16 * n0, (cuuint64_t)16 * n0 * n1};   // bytes, multiples of 16
+    const cuuint32_t box[3] = {(cuuint32_t)boxx, (cuuint32_t)boxy, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = rb_encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(x), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TDZ_CHECK(r == CUDA_SUCCESS, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
 bool tune_lookup(const TuneKey &k, int *txw, int *zchunk) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(k);
@@ -171,6 +225,7 @@ void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, v
         prm.red = ex.red;
         prm.dotv = ex.dotv;
         prm.red_mode = ex.red_mode;
+        prm.err = apply_error_word();
         return prm;
     };
     if (dim == 1) {
@@ -178,6 +233,7 @@ void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, v
         if (prec != TDZ_FP32) launch_1d(params(double{}), st);
         else launch_1d(params(float{}), st);
     } else {
+        TDZ_CHECK(prec != kPrecF32M64 || dim == 3, TDZ_ERR_INTERNAL, "FP32 arithmetic on FP64 vectors is 3D only");
         ApplyParams<float> pf{};
         ApplyParams<double> pd{};
         ApplyParams<dff> pdf{};

@@ -53,6 +53,7 @@ template <class T> struct ApplyParams {
     double2 *red;
     const void *dotv;
     int red_mode;
+    int *err;                   // error word of bounded waits (device, library-owned)
 };
 
 
@@ -646,26 +647,8 @@ inline void run2d(const ApplyParams<T> &prm0, cudaStream_t st) {
     k_apply2d<T, P, HB, HC, kTX2><<<grid, kTX2, 0, st>>>(prm);
 }
 
-template <class T, int P>
-inline void dispatch_streams(int dim, bool hb, bool hc, const ApplyParams<T> &prm, cudaStream_t st) {
-    if (dim == 3) {
-        if constexpr (std::is_same<T, dff>::value) {
-            if (!hb && hc && prm.zc_kind == 2) { run3d<T, P, false, true, 0, 2>(prm, st); return; }   // CN stage
-            if (!hb && !hc && prm.za_kind == 1) { run3d<T, P, false, false, 1, 0>(prm, st); return; }  // mass
-        }
-        if (hb && hc) run3d<T, P, true, true>(prm, st);
-        else if (hb) run3d<T, P, true, false>(prm, st);
-        else if (hc) run3d<T, P, false, true>(prm, st);
-        else run3d<T, P, false, false>(prm, st);
-    } else {
-        if (hb && hc) run2d<T, P, true, true>(prm, st);
-        else if (hb) run2d<T, P, true, false>(prm, st);
-        else if (hc) run2d<T, P, false, true>(prm, st);
-        else run2d<T, P, false, false>(prm, st);
-    }
-}
-
 // per-degree entry points (apply_p<P>.cu)
+// (prec: TDZ_FP32, TDZ_FP64, TDZ_FP64_DF, or kPrecF32M64 with pf on FP64 vectors)
 #define TDZ_APPLY_DECL(P)                                                                                  \
     void apply_p##P(int dim, bool hb, bool hc, const ApplyParams<float> &pf, const ApplyParams<double> &pd, \
                     const ApplyParams<dff> &pdf, int prec, cudaStream_t st);

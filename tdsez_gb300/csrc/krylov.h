@@ -47,17 +47,22 @@ struct FGMRES {
     long long applies = 0;
     long long early_accepts = 0;   // iterations that met the target after one Gram-Schmidt pass
     int aprec = TDZ_FP64;   // operator apply arithmetic: TDZ_FP64 or TDZ_FP64_DF (FP64 vectors either way)
-    // Relaxed Arnoldi applies (inexact Krylov): A z_j in FP32 while the
-    // residual r0 = b - A x of every restart stays in aprec. A cycle that
-    // reports convergence is accepted when the estimate plus the a-posteriori
-    // bound sum_j |y_j| 1e-4 ||A z_j|| on its distance from the true residual
-    // meets the target (the FP32 errors enter scaled by the small y_j once the
-    // start residual is small); otherwise one more restart, whose aprec
-    // residual decides. A relaxed cycle that fails to cut the true residual
-    // tenfold switches the solve back to exact applies.
+    // Relaxed Arnoldi applies (inexact Krylov): A z_j in FP32 arithmetic
+    // while the residual r0 = b - A x of every restart stays in aprec. The
+    // FP32 apply's error is bounded elementwise by gamma |A| |z_j| (gamma =
+    // k u / (1 - k u), u = 2^-24, k the accumulation depth of the three band
+    // stages plus the input and band roundings), so the true residual of the
+    // cycle differs from its estimate by at most
+    //   sum_j |y_j| gamma || |A| || ||z_j||,
+    // with || |A| || bounded from the Kronecker factors (abs_norm_bound). A
+    // cycle that reports convergence is accepted when the estimate plus that
+    // bound meets the target; otherwise one more restart, whose aprec residual
+    // decides. A relaxed cycle that fails to cut the true residual tenfold
+    // switches the solve back to exact applies.
     bool relaxed = false;
     DevBuf z32, w32;
     long long relaxed_applies = 0;
+    long long relaxed_accepts = 0;   // solves that ended on a certified relaxed cycle
 
     void setup(Operator *op_, int restart_, Precond *pc_);
     // Solve A x = b (A = the operator's current stage, FP64), x holds the guess.

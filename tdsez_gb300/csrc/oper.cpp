@@ -175,6 +175,27 @@ std::vector<Term> Operator::terms_for(int which) const {
     return out;
 }
 
+double Operator::abs_norm_bound(int which) const {
+    const std::array<cd, 5> sg = sigma_for(which);
+    double total = 0.0;
+    for (const Term &t : terms_for(which)) {
+        double f = std::abs(t.factor * sg[t.scalar]);
+        if (f == 0.0) continue;
+        for (int d = 0; d < sp->dim; ++d) {
+            const BandD &b = bases[d][t.band[d]];
+            double mx = 0.0;
+            for (int i = 0; i < b.n; ++i) {
+                double rs = 0.0;
+                for (int o = 0; o < b.bw(); ++o) rs += std::abs(b.v[(size_t)i * b.bw() + o]);
+                mx = std::max(mx, rs);
+            }
+            f *= mx;
+        }
+        total += f;
+    }
+    return total;
+}
+
 std::array<cd, 5> Operator::sigma_for(int which) const {
     if (which == TDZ_STAGE) return sigma;
     std::array<cd, 5> s{cd(0), cd(0), cd(0), cd(0), cd(0)};
@@ -281,8 +302,8 @@ void ensure_red(Operator &op) {
 }  // namespace
 
 void Operator::residual(int which, int prec, const void *x, const void *b, void *y, cudaStream_t st, double *norm) {
-    TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG,
-              "precision must be TDZ_FP32, TDZ_FP64 or TDZ_FP64_DF");
+    TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64 || prec == TDZ_FP64_DF || (prec == kPrecF32M64 && f32_on_f64()),
+              TDZ_ERR_ARG, "precision must be TDZ_FP32, TDZ_FP64, TDZ_FP64_DF or (3D, no soft-core term) TDZ_FP64_F32");
     TDZ_CHECK(x && y, TDZ_ERR_ARG, "null vector");
     TDZ_CHECK(x != y, TDZ_ERR_ARG, "x and y must not alias");
     if (which == TDZ_STAGE) TDZ_CHECK(stage_set, TDZ_ERR_STATE, "stage coefficients not set");
@@ -308,17 +329,16 @@ void Operator::residual(int which, int prec, const void *x, const void *b, void 
             const double v = take_reduction(*this, st).real();
             *norm = std::isfinite(v) ? std::sqrt(std::max(0.0, v)) : std::numeric_limits<double>::quiet_NaN();
         } else {
-            blas::Reducer red;
             *norm = blas::nrm2(red, y, (size_t)sp->ndof(), prec == TDZ_FP32 ? TDZ_FP32 : TDZ_FP64, st);
         }
     }
 }
 
 void Operator::apply_dot(int which, int prec, const void *x, void *y, const void *v, cd *dot, cudaStream_t st) {
-    TDZ_CHECK(prec == TDZ_FP64 || prec == TDZ_FP64_DF, TDZ_ERR_ARG, "apply_dot works on FP64 vectors");
+    TDZ_CHECK(prec == TDZ_FP64 || prec == TDZ_FP64_DF || prec == kPrecF32M64, TDZ_ERR_ARG,
+              "apply_dot works on FP64 vectors");
     if (!fused_reductions()) {
         apply(which, prec, x, y, st);
-        blas::Reducer red;
         const void *V[1] = {v};
         blas::mdot(red, V, 1, y, (size_t)sp->ndof(), TDZ_FP64, dot, st);
         return;
@@ -352,7 +372,6 @@ void Operator::observables(const double2 *psi, std::vector<cd> &out, cudaStream_
         apply(which[i], TDZ_FP64_DF, psi, obs_buf[i].ptr, st);
         V[i] = obs_buf[i].ptr;
     }
-    blas::Reducer red;
     std::vector<cd> d(k);
     blas::mdot(red, V.data(), k, psi, n, TDZ_FP64, d.data(), st);   // conj(A psi) . psi
     out.resize(k);

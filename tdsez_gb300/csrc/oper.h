@@ -7,12 +7,16 @@
 #include <memory>
 #include <vector>
 
+#include "blas.h"
 #include "quad.h"
 #include "space.h"
 
 namespace tdz {
 
 constexpr int kMaxComb = 8;   // base bands in one combination
+// internal name of TDZ_FP64_F32: FP32 arithmetic on FP64 vectors (3D
+// operators without the quadrature term), the certified FP32 Arnoldi apply
+constexpr int kPrecF32M64 = TDZ_FP64_F32;
 
 // coef * (band[2] (x) band[1] (x) band[0]); band ids index the per-axis base
 // band lists of the operator. The coefficient is factor * sigma[scalar] with
@@ -83,7 +87,15 @@ struct Operator {
     // y = op x and *dot = <v, y> = sum conj(v) y (FP64 vectors; synchronises)
     void apply_dot(int which, int prec, const void *x, void *y, const void *v, cd *dot, cudaStream_t st);
     DevBuf red_part, red_res;      // fused-reduction partials and result
+    blas::Reducer red;             // unfused reductions (allocated on first use, then reused)
     bool fused_reductions() const;
+    // upper bound on || |A| ||_2 for operator `which` at the current stage:
+    // sum over Kronecker terms of |coefficient| times the product of the
+    // terms' 1D max absolute row sums (|A| is symmetric, so its 2-norm is at
+    // most its infinity norm); the quadrature term is not included
+    double abs_norm_bound(int which) const;
+    // FP32 arithmetic on FP64 vectors available (3D, no quadrature term)
+    bool f32_on_f64() const { return sp->dim == 3 && !quad.on; }
     // <psi|M|psi>, <psi|H|psi>, <psi|D_a|psi> (FP64 psi); see tdz_observables
     std::vector<DevBuf> obs_buf;
     void observables(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
@@ -112,5 +124,8 @@ struct ApplyExtra {
 };
 void launch_apply(const Operator &op, const Plan &pl, int prec, const void *x, void *y, cudaStream_t st,
                   const ApplyExtra &ex = ApplyExtra{});
+// error word of the 3D apply kernels (a bounded wait that ran out), read and
+// cleared (synchronises the device)
+int take_apply_error();
 
 }  // namespace tdz

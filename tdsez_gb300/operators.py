@@ -131,9 +131,11 @@ class Operator:
         _lib.check(_lib.load().tdz_operator_set_stage(self.handle, complex(alpha).real, complex(alpha).imag,
                                                       complex(g).real, complex(g).imag, len(c), arr))
 
-    def apply(self, which: int, x, y, stream=None, df: bool = False):
-        """y = op x on torch complex64 / complex128 CUDA tensors. ``df``: on
-        complex128, compute in double-float arithmetic (TDZ_FP64_DF)."""
+    def apply(self, which: int, x, y, stream=None, df: bool = False, f32: bool = False):
+        """y = op x on torch complex64 / complex128 CUDA tensors. On
+        complex128: ``df`` computes in double-float arithmetic (TDZ_FP64_DF),
+        ``f32`` in FP32 arithmetic (TDZ_FP64_F32, 3D without soft-core
+        centres)."""
         import torch
         if x.dtype != y.dtype or x.dtype not in (torch.complex64, torch.complex128):
             raise TypeError("x and y must both be complex64 or complex128")
@@ -144,6 +146,8 @@ class Operator:
         prec = _lib.TDZ_FP64 if x.dtype == torch.complex128 else _lib.TDZ_FP32
         if df and prec == _lib.TDZ_FP64:
             prec = _lib.TDZ_FP64_DF
+        elif f32 and prec == _lib.TDZ_FP64:
+            prec = _lib.TDZ_FP64_F32
         s = torch.cuda.current_stream().cuda_stream if stream is None else stream
         _lib.check(_lib.load().tdz_operator_apply(self.handle, which, prec, C.c_void_p(x.data_ptr()),
                                                   C.c_void_p(y.data_ptr()), C.c_void_p(s)))

@@ -25,7 +25,7 @@ NEL = (136, 24, 96)
 # None: the autotuned shape; (16, 133): the shape the tuner picks on the
 # 160 x 160 x 320 workload for the double-float stage apply
 SHAPES = [None, (16, 133), (16, 20), (28, 64), (32, 300)]
-TOL = {"fp64": 1e-12, "df": 1e-12, "fp32": 1e-6}
+TOL = {"fp64": 1e-12, "df": 1e-12, "fp32": 1e-6, "f32": 1e-6}
 
 
 @pytest.fixture(scope="module")
@@ -67,11 +67,12 @@ def test_stage_and_mass_apply_at_bench_shapes(mid, shape):
             op.set_stage(alpha, g, cc)
             ref_a = oo.kron_apply(S, oo.kron_terms(S, ph, g=g, c=cc, alpha=alpha), x)
             ref_m = oo.kron_apply(S, oo.kron_terms(S, ph, g=0.0, alpha=1.0)[:1], x)
-            for prec, dt in (("fp64", torch.complex128), ("df", torch.complex128), ("fp32", torch.complex64)):
+            for prec, dt in (("fp64", torch.complex128), ("df", torch.complex128), ("fp32", torch.complex64),
+                             ("f32", torch.complex128)):
                 xd = torch.tensor(x, dtype=dt, device="cuda")
                 for which, ref in ((_lib.TDZ_STAGE, ref_a), (_lib.TDZ_MASS, ref_m)):
                     yd = torch.full_like(xd, float("nan"))
-                    op.apply(which, xd, yd, df=prec == "df")
+                    op.apply(which, xd, yd, df=prec == "df", f32=prec == "f32")
                     torch.cuda.synchronize()
                     err = _rel(yd.cpu().numpy().astype(np.complex128), ref)
                     assert err < TOL[prec], (shape, g, prec, which, err)
@@ -80,11 +81,13 @@ def test_stage_and_mass_apply_at_bench_shapes(mid, shape):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("relaxed", [False, True])
 @pytest.mark.parametrize("shape", [None, (16, 133)])
-def test_cn_step_at_bench_shapes(mid, shape):
+def test_cn_step_at_bench_shapes(mid, shape, relaxed):
     """One CN step exactly as the bench runs it (FP32 fast-diagonalisation
-    preconditioner, double-float FGMRES applies with the fused residual,
-    norm and dot reductions, x0 = P^-1 b, the fused CN update), then the
+    preconditioner, double-float FGMRES residuals with the fused norm,
+    x0 = P^-1 b, the fused CN update; the Arnoldi apply in double-float or,
+    relaxed, in FP32 arithmetic certified by its error bound), then the
     stage system re-evaluated by the oracle in FP64."""
     import torch
     from tdsez_gb300.propagator import Propagator
@@ -96,7 +99,8 @@ def test_cn_step_at_bench_shapes(mid, shape):
         rng = np.random.default_rng(23)
         noise = torch.tensor(1e-3 * (rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)), device="cuda")
         psi0 = psi0 + noise
-        G = Propagator(op, "cn", field=w.field, pc="fdm", precision="fp32", rtol=1e-10, outer="df", guess_order=-1)
+        G = Propagator(op, "cn", field=w.field, pc="fdm", precision="fp32", rtol=1e-10, outer="df", guess_order=-1,
+                       relaxed=relaxed)
         t, dt = 200.0, w.dt
         psi = psi0.clone()
         G.step(psi, t, dt)
