@@ -464,6 +464,105 @@ def cpu_baseline(n_full: int, dt: float, seconds: float):
             % (r["steps"], r["elements"], r["ndof"], how, r["seconds"], r["ndof"], n_full)}
 
 
+def _timed_steps(G, psi, t0, dt, warmup, steps, stream):
+    """warmup untimed steps, then `steps` steps between CUDA events; returns
+    (steps/s, Krylov its per stage solve, t after the steps)."""
+    import torch
+    t = t0
+    for _ in range(warmup):
+        G.step(psi, t, dt)
+        t += dt
+    torch.cuda.synchronize()
+    s0 = G.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        G.step(psi, t, dt)
+        t += dt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s1 = G.stats()
+    el = e0.elapsed_time(e1) / 1e3
+    return steps / el, (s1["its"] - s0["its"]) / max(1, s1["solves"] - s0["solves"]), t
+
+
+def run_softcore(args):
+    """The soft-core configurations at size (secondary lines, not the
+    headline): cfg2, 2D soft-core hydrogen 512^2 elements p = 4, Pade(2,2)
+    dt = 0.02 with a CAP of width 20 a.u. and t-SURFF on |x_d| = 80, ground
+    state by the GPU eigensolver, FP32 multigrid inside FP64 FGMRES against
+    the FP64 multigrid; cfg3, 3D soft-core atom 192^3 elements p = 4 with
+    symmetric exponential knots, Magnus-4 dt = 0.02, 3-level multigrid in
+    FP32 inside FP64 FGMRES. Steps are timed with CUDA events after
+    --warmup untimed steps, starting at the pulse's peak."""
+    import dataclasses
+    import torch
+    from tdsez_gb300 import _lib as L
+    from tdsez_gb300 import build as _build
+    from tdsez_gb300.eigen import bound_states
+    from tdsez_gb300.operators import Operator
+    from tdsez_gb300.propagator import Propagator
+    from tdsez_gb300.space import Space
+    from tdsez_gb300.tsurff import TSurff
+    from tdsez_gb300.workloads import softcore2d, softcore3d
+    torch.cuda.set_device(0)
+    _build.build()
+    L.load()
+    stream = torch.cuda.current_stream()
+    out = {"config": args.config, "unit": "steps/s", "data": "synthetic (seeded workload, ground state or packet)"}
+    if args.config == "cfg2":
+        w = softcore2d(nel=args.nel or 512)
+        S = Space(w.knots, w.p, w.nq)
+        op = Operator(S, w.phys)
+        op0 = Operator(S, dataclasses.replace(w.phys, cap_kmin=None, bounds=()))
+        torch.cuda.synchronize()
+        tg = time.time()
+        E, V, berr, solves = bound_states(op0, 1, target=-1.5, tol=1e-10, pc="mg", precision="fp32", rtol=1e-11,
+                                          outer="df")
+        torch.cuda.synchronize()
+        out["ground_state"] = {"E0": E[0], "backward_error": berr[0], "inner_solves": solves,
+                               "seconds": time.time() - tg}
+        psi0 = V[0].clone()
+        t0 = 0.5 * w.meta["T"]
+        arms = {}
+        for name, kw in (("fp32_mg_in_fp64", dict(pc="mg", precision="fp32", outer="df")),
+                         ("fp64_mg", dict(pc="mg", precision="fp64", outer="fp64"))):
+            G = Propagator(op, "pade22", field=w.field, rtol=args.rtol, **kw)
+            psi = psi0.clone()
+            sps, its, _ = _timed_steps(G, psi, t0, w.dt, args.warmup, args.steps if "fp32" in name else
+                                       max(2, args.steps // 4), stream)
+            arms[name] = {"steps_per_s": sps, "its_per_solve": its}
+        ts = TSurff(S, 80.0, [(-2.0, 2.0, 128)] * 2, w.field, w.dt)
+        ts.sample(t0, psi)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(10):
+            ts.sample(t0 + (k + 1) * w.dt, psi)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.update({"workload": "2D soft-core 512^2 el p=4, Pade(2,2) dt=0.02, CAP 20 a.u., t-SURFF R=80",
+                    "ndof": S.ndof, "arms": arms, "tsurff_sample_ms": e0.elapsed_time(e1) / 10,
+                    "rtol": args.rtol})
+    else:
+        w = softcore3d(nel=args.nel or 192)
+        S = Space(w.knots, w.p, w.nq)
+        op = Operator(S, w.phys)
+        psi = op.separable_state(w.packet)
+        t0 = 0.5 * w.meta["T"]
+        G = Propagator(op, "magnus4", field=w.field, rtol=args.rtol, pc="mg", precision="fp32", outer="df",
+                       mg_levels=3)
+        sps, its, _ = _timed_steps(G, psi, t0, w.dt, args.warmup, args.steps, stream)
+        op.set_stage(1.0, 0.01j, [0.001])
+        x32 = psi.to(torch.complex64)
+        y32 = torch.empty_like(x32)
+        ta = time_kernel(lambda: op.apply(L.TDZ_STAGE, x32, y32), 5, stream)
+        out.update({"workload": "3D soft-core 192^3 el p=4 symexp, Magnus-4 dt=0.02, 3-level MG (FP32) in FP64 FGMRES",
+                    "ndof": S.ndof, "steps_per_s": sps, "its_per_solve": its, "rtol": args.rtol,
+                    "fp32_stage_apply_us": ta * 1e6, "fp32_stage_apply_gbs": 16.0 * S.ndof / ta / 1e9})
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -504,9 +603,14 @@ def main():
     ap.add_argument("--mg-levels", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="cfg5", choices=["cfg5", "cfg2", "cfg3"],
+                    help="cfg5: the headline heterostructure; cfg2 / cfg3: the soft-core configurations at size")
+    ap.add_argument("--nel", type=int, default=0, help="elements per axis of cfg2 / cfg3 (0: the configuration's)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config in ("cfg2", "cfg3"):
+        run_softcore(args)
     elif args.batch_scan > 0:
         batch_scan(args)
     else:

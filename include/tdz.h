@@ -334,6 +334,28 @@ tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, 
 tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds);
 void tdz_prop_destroy(tdz_prop *p);
 
+/* -------------------------------------------------------------- bound states
+ * nev eigenpairs of H c = E M c nearest `target`, in FP64 on the device: the
+ * SLEPc Krylov-Schur shift-invert GHEP solve of src/core.cpp:887-1048
+ * (shift 1e-3 max(1, |target|) below the target, Krylov-Schur in its
+ * Hermitian form: thick-restart Lanczos on (H - s M)^-1 M in the M inner
+ * product; inner solves by this library's FGMRES with `inner`'s
+ * preconditioner on the stage alpha = -s, g = 1, or, with inner = NULL, the
+ * FDM inverse in 3D and the multigrid otherwise, rtol 1e-11). vecs: nev FP64
+ * device vectors of ndof coefficients each, back to back; on entry vecs[0]
+ * holds a start vector (its real part is used: any real vector not
+ * M-orthogonal to the wanted states), on return the M-normalised
+ * eigenvectors in ascending energy. energies (host, nev), berr (host, may be
+ * NULL): the backward errors ||H v - E M v|| / ((||H|| + |E| ||M||) ||v||)
+ * of TDSEZBackwardError (src/core.cpp:474-492) with native FP64 applies and
+ * upper bounds of the norms; the reference accepts 1e-8. The Lanczos run
+ * stops when every wanted Ritz residual estimate is below tol |theta|, or
+ * fails (TDZ_ERR_NOT_CONVERGED) after maxit inner solves. The operator must
+ * carry no absorbing layer (H Hermitian); its stage coefficients are
+ * overwritten. */
+tdz_status tdz_eigen_solve(tdz_op *op, int nev, double target, double tol, int maxit, const tdz_solver_opts *inner,
+                           void *vecs, double *energies, double *berr, int *solves, void *stream);
+
 /* Preconditioner refresh rule of TDSEZPCRefresh::Stale
  * (include/tdsez_propagator.hpp:17-31): the preconditioner built from one
  * stage is reused; the first solve after a build sets base, and a solve

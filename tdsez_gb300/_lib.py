@@ -127,6 +127,7 @@ SIGNATURES = {
     "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
     "tdz_set_autotune": (None, [I]),
     "tdz_set_apply3d_shape": (None, [I, I]),
+    "tdz_eigen_solve": (I, [VP, I, D, D, I, C.c_void_p, VP, C.POINTER(D), C.POINTER(D), C.POINTER(I), VP]),
     "tdz_prop_refreshes": (I, [VP, C.POINTER(LL)]),
     "tdz_pc_refresh_stale": (I, [C.POINTER(tdz_pc_refresh), I]),
     "tdz_strong_field_ratio": (I, [VP, I, D, D, FIELD_FN, VP, C.POINTER(D)]),

@@ -459,6 +459,30 @@ tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, 
     });
 }
 
+tdz_status tdz_eigen_solve(tdz_op *op, int nev, double target, double tol, int maxit, const tdz_solver_opts *inner,
+                           void *vecs, double *energies, double *berr, int *solves, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(op && vecs && energies, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(tol > 0.0 && maxit > 0, TDZ_ERR_ARG, "tol and maxit must be positive");
+        TDZ_CHECK(reinterpret_cast<uintptr_t>(vecs) % 16 == 0, TDZ_ERR_ARG, "vecs must be 16-byte aligned");
+        tdz::SolverOptions so;
+        if (inner) {
+            so = solver_options(inner);
+        } else {   // exact FDM inverse for 3D, multigrid otherwise; FP32 inside FP64 FGMRES
+            so.pc = op->o.sp->dim == 3 ? TDZ_PC_FDM : TDZ_PC_MG;
+            so.rtol = 1e-11;
+            so.outer = TDZ_FP64_DF;
+        }
+        const tdz::EigenResult r = tdz::eigen_solve(op->o, nev, target, tol, maxit, so, static_cast<double2 *>(vecs),
+                                                    static_cast<cudaStream_t>(stream));
+        for (int i = 0; i < nev; ++i) {
+            energies[i] = r.energies[i];
+            if (berr) berr[i] = r.berr[i];
+        }
+        if (solves) *solves = r.solves;
+    });
+}
+
 tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds) {
     return guarded([&] {
         TDZ_CHECK(p && rebuilds, TDZ_ERR_ARG, "null argument");

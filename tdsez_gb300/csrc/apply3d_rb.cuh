@@ -288,21 +288,34 @@ __device__ __noinline__ double2 rb_run(const ApplyParams<T> &prm, const CUtensor
         else return reinterpret_cast<const C *>(landp(it % 3));
     };
     // x stage of plane it: tile(it) -> sU[it & 1]
+    // (the thread's rows ty, ty + NTY, ... are unrolled together, so their
+    // independent accumulation chains interleave)
+    constexpr int XR = (RY + NTY - 1) / NTY;
     auto xstage = [&](int it) {
         const C *in = tile(it);
         const int buf = it & 1;
-        for (int q = ty; q < RY; q += NTY) {
-            C uM = czero<C>(), uT = czero<C>(), uS = czero<C>();
+        C uM[XR], uT[XR], uS[XR];
 #pragma unroll
-            for (int j = 0; j < BW; ++j) {
+        for (int k = 0; k < XR; ++k) { uM[k] = czero<C>(); uT[k] = czero<C>(); uS[k] = czero<C>(); }
+#pragma unroll
+        for (int j = 0; j < BW; ++j) {
+#pragma unroll
+            for (int k = 0; k < XR; ++k) {
+                const int q = ty + k * NTY;
+                if (k == XR - 1 && q >= RY) break;
                 const C v = in[q * RX + tx + j];
-                rfma(uM, xm[j], v);
-                if constexpr (HB) cfma(uT, xt[j], v);
-                if constexpr (HC) rfma(uS, xs[j], v);
+                rfma(uM[k], xm[j], v);
+                if constexpr (HB) cfma(uT[k], xt[j], v);
+                if constexpr (HC) rfma(uS[k], xs[j], v);
             }
-            up(buf, 0, q)[tx] = cnorm(uM);
-            if constexpr (HB) up(buf, UT, q)[tx] = cnorm(uT);
-            if constexpr (HC) up(buf, US, q)[tx] = cnorm(uS);
+        }
+#pragma unroll
+        for (int k = 0; k < XR; ++k) {
+            const int q = ty + k * NTY;
+            if (k == XR - 1 && q >= RY) break;
+            up(buf, 0, q)[tx] = cnorm(uM[k]);
+            if constexpr (HB) up(buf, UT, q)[tx] = cnorm(uT[k]);
+            if constexpr (HC) up(buf, US, q)[tx] = cnorm(uS[k]);
         }
     };
     // y and z stages of plane it; output plane zs + it - P + o of row r

@@ -424,6 +424,19 @@ void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st) {
     count_launch();
 }
 
+namespace {
+__global__ void k_keep_real(double2 *x, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        x[i].y = 0.0;
+}
+}  // namespace
+
+void keep_real(void *x, size_t n, cudaStream_t st) {
+    k_keep_real<<<grid_for(n), kThreads, 0, st>>>(static_cast<double2 *>(x), n);
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
+}
+
 void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st) {
     k_add_cast_df<<<grid_for(n), kThreads, 0, st>>>(y, cdf_host(a), x, n);
     TDZ_CUDA(cudaGetLastError());

@@ -21,6 +21,8 @@ void axpby(void *y, cd a, const void *x, cd b, size_t n, int prec, cudaStream_t 
 void axpbypcz(void *y, cd a, const void *x, cd b, const void *z, cd c, size_t n, int prec, cudaStream_t st);
 // y (precision py) = x (precision px)
 void cast(const void *x, int px, void *y, int py, size_t n, cudaStream_t st);
+// x <- Re(x) (FP64: imaginary parts set to zero)
+void keep_real(void *x, size_t n, cudaStream_t st);
 // y64 += a * x32 (FP32 correction added to an FP64 vector)
 void add_cast(double2 *y, cd a, const float2 *x, size_t n, cudaStream_t st);
 

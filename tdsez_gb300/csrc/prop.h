@@ -89,4 +89,16 @@ struct Propagator {
                      double2 *cn_psi = nullptr, bool *cn_done = nullptr);
 };
 
+// Bound states of H c = E M c nearest a target (eigen.cpp)
+struct EigenResult {
+    std::vector<double> energies, berr;   // ascending energies and their backward errors
+    int solves = 0, restarts = 0;
+    long long inner_its = 0;
+};
+// nev eigenpairs nearest `target`; vecs: nev FP64 device vectors (in: a start
+// vector in vecs[0], its real part is used; out: M-normalised eigenvectors);
+// Lanczos stops when the Ritz residual estimates are below tol |theta|
+EigenResult eigen_solve(Operator &op, int nev, double target, double tol, int maxit, const SolverOptions &so,
+                        double2 *vecs, cudaStream_t st);
+
 }  // namespace tdz
