@@ -408,6 +408,17 @@ tdz_status tdz_tsurff_create(const tdz_space *s, const tdz_tsurff_opts *o, tdz_f
 tdz_status tdz_tsurff_sample(tdz_tsurff *ts, double t, const void *psi, void *stream);
 /* Accumulated amplitudes b(k), prod(nk) complex values (host array). */
 tdz_status tdz_tsurff_amplitudes(tdz_tsurff *ts, double *out, void *stream);
+/* Projection of psi (FP64 device vector, normally psi(T)) inside the box
+ * |x_d| < R onto the Volkov states at the last sample time: the interior term
+ * of TDSEZTSurff::Interior / Project (src/tsurff.cpp:565-639),
+ *   phi(k) sum_ijl c_ijl F_x[k_x][i] F_y[k_y][j] F_z[k_z][l],
+ *   F_d[k][i] = sum_q w_q exp(-i (k + A_d) x_q) B_i(x_q) over the in-box nodes,
+ *   phi(k) = (2 pi)^(-d/2) exp(i (C + T |k|^2 / 2m + k.B / m)),
+ * with the axis contractions on the device (double-float arithmetic). Adding
+ * it to tdz_tsurff_amplitudes gives the spectrum of a run that ends before
+ * all of the wave packet has left the box. out (host): prod(nk) complex
+ * values, k_x slowest. Synchronises the stream. */
+tdz_status tdz_tsurff_interior(tdz_tsurff *ts, const void *psi, double *out, void *stream);
 /* Volkov integrals at the last sample: A[3], B[3], C, t (8 doubles). */
 tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct);
 void tdz_tsurff_destroy(tdz_tsurff *ts);

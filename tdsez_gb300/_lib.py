@@ -122,6 +122,7 @@ SIGNATURES = {
     "tdz_tsurff_sample": (I, [VP, D, VP, VP]),
     "tdz_tsurff_amplitudes": (I, [VP, C.POINTER(D), VP]),
     "tdz_tsurff_volkov": (I, [VP, C.POINTER(D)]),
+    "tdz_tsurff_interior": (I, [VP, VP, C.POINTER(D), VP]),
     "tdz_tsurff_destroy": (None, [VP]),
     "tdz_solver_train_coarse": (I, [VP, I, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), VP]),
     "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),

@@ -556,6 +556,15 @@ tdz_status tdz_tsurff_amplitudes(tdz_tsurff *ts, double *out, void *stream) {
     });
 }
 
+tdz_status tdz_tsurff_interior(tdz_tsurff *ts, const void *psi, double *out, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(ts && psi && out, TDZ_ERR_ARG, "null argument");
+        std::vector<tdz::cd> v;
+        ts->t.interior(static_cast<const double2 *>(psi), v, static_cast<cudaStream_t>(stream));
+        for (size_t i = 0; i < v.size(); ++i) { out[2 * i] = v[i].real(); out[2 * i + 1] = v[i].imag(); }
+    });
+}
+
 tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct) {
     return guarded([&] {
         TDZ_CHECK(ts && abct, TDZ_ERR_ARG, "null argument");

@@ -225,6 +225,8 @@ void TSurff::setup(const Space &s, const tdz_tsurff_opts &o, tdz_field_fn f, voi
             upload(T.off, off);
             upload(T.val, val);
             upload(T.der, der);
+            hoff[d] = off;
+            hval[d].assign(val.begin(), val.end());
             for (int side = 0; side < 2; ++side) {
                 const double x = side ? R : -R;
                 const int sp = find_span(A.U, A.p, A.n, x);
@@ -372,6 +374,85 @@ void TSurff::sample(double t, const double2 *psi, cudaStream_t st) {
     prevT = t;
     have_prev = true;
     ++samples;
+}
+
+namespace {
+// out[a][k][b] = sum_i F[k][i] in[a][i][b] (complex, double-float arithmetic)
+__global__ void k_axis_dense(const double2 *__restrict__ F, const double2 *__restrict__ in, double2 *__restrict__ out,
+                             long long A, int nk, int ni, long long B) {
+    const long long total = A * nk * B;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long b = t % B, r = t / B;
+        const int k = (int)(r % nk);
+        const long long a = r / nk;
+        cdff acc;
+        acc.x = dff(0.f);
+        acc.y = dff(0.f);
+        const double2 *fk = F + (size_t)k * ni;
+        const double2 *ia = in + (size_t)a * ni * B + b;
+        for (int i = 0; i < ni; ++i) {
+            const cdff f = load_c<cdff, double2>(fk[i]);
+            const cdff v = load_c<cdff, double2>(ia[(size_t)i * B]);
+            cfma(acc, f, v);
+        }
+        out[t] = store_c<double2, cdff>(cnorm(acc));
+    }
+}
+}  // namespace
+
+void TSurff::interior(const double2 *psi, std::vector<cd> &out, cudaStream_t st) {
+    // F_d[k][i] = sum_q w_q exp(-i (k + A_d) x_q) B_i(x_q) over the in-box nodes
+    for (int d = 0; d < 3; ++d) {
+        std::vector<double2> f((size_t)nk[d] * n[d], make_double2(0.0, 0.0));
+        if (d >= dim) {
+            f[0] = make_double2(1.0, 0.0);
+        } else {
+            const int pp = ax[d].p + 1;
+            for (size_t q = 0; q < nodes[d].size(); ++q)
+                for (int kk = 0; kk < nk[d]; ++kk) {
+                    const double ph = -(k[d][kk] + A[d]) * nodes[d][q];
+                    const cd e = weights[d][q] * cd(std::cos(ph), std::sin(ph));
+                    for (int b = 0; b < pp; ++b) {
+                        const int i = hoff[d][q] + b;
+                        const cd v = e * hval[d][q * pp + b];
+                        double2 &z = f[(size_t)kk * n[d] + i];
+                        z.x += v.real();
+                        z.y += v.imag();
+                    }
+                }
+        }
+        upload(F[d], f);
+    }
+    // contract x, then y, then z: [z][y][x] -> [z][y][kx] -> [z][ky][kx] -> [kz][ky][kx]
+    const size_t w0 = (size_t)n[2] * n[1] * nk[0], w1 = (size_t)n[2] * nk[1] * nk[0];
+    if (work[0].bytes < w0 * sizeof(double2)) work[0].alloc(w0 * sizeof(double2));
+    if (work[1].bytes < std::max(w1, nktot) * sizeof(double2)) work[1].alloc(std::max(w1, nktot) * sizeof(double2));
+    auto pass = [&](const double2 *src, double2 *dst, long long a, int d, long long b) {
+        const long long total = a * nk[d] * b;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 16LL * sm_count());
+        k_axis_dense<<<blocks, 256, 0, st>>>(F[d].as<double2>(), src, dst, a, nk[d], n[d], b);
+        TDZ_CUDA(cudaGetLastError());
+        count_launch();
+    };
+    pass(psi, work[0].as<double2>(), (long long)n[2] * n[1], 0, 1);
+    pass(work[0].as<double2>(), work[1].as<double2>(), n[2], 1, nk[0]);
+    pass(work[1].as<double2>(), work[0].as<double2>(), 1, 2, (long long)nk[1] * nk[0]);
+    std::vector<double2> h(nktot);
+    TDZ_CUDA(cudaMemcpyAsync(h.data(), work[0].ptr, nktot * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    TDZ_CUDA(cudaStreamSynchronize(st));
+    // times the Volkov phase (2 pi)^(-d/2) exp(i (C + T k^2 / 2m + k.B / m)), k_x slowest
+    const double norm = std::pow(2.0 * M_PI, -0.5 * dim);
+    out.assign(nktot, cd(0.0));
+    for (int i = 0; i < nk[0]; ++i)
+        for (int j = 0; j < nk[1]; ++j)
+            for (int l = 0; l < nk[2]; ++l) {
+                const double kv[3] = {k[0][i], k[1][j], k[2][l]};
+                double ph = C;
+                for (int d = 0; d < dim; ++d) ph += vt * kv[d] * kv[d] / (2.0 * mass) + kv[d] * B[d] / mass;
+                const double2 g = h[((size_t)l * nk[1] + j) * nk[0] + i];
+                out[((size_t)i * nk[1] + j) * nk[2] + l] = norm * cd(std::cos(ph), std::sin(ph)) * cd(g.x, g.y);
+            }
 }
 
 }  // namespace tdz

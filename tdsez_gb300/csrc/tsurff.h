@@ -39,7 +39,15 @@ struct TSurff {
     long long samples = 0;
     int n[3] = {1, 1, 1};
 
+    // host copies of the in-box node tables (first basis index, p+1 values per node)
+    std::array<std::vector<int>, 3> hoff;
+    std::array<std::vector<double>, 3> hval;
+    DevBuf F[3], work[2];               // interior projection: per-axis tables and work arrays
+
     void setup(const Space &s, const tdz_tsurff_opts &o, tdz_field_fn f, void *ctx);
+    // <chi_k(t_last) | theta psi> over the box |x_d| < R (TDSEZTSurff::Interior /
+    // Project, src/tsurff.cpp:565-639): out (host) nk complex values, k_x slowest
+    void interior(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
     void advance_volkov(double t);
     void sample(double t, const double2 *psi, cudaStream_t st);
 };

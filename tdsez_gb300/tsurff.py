@@ -50,6 +50,17 @@ class TSurff:
         _lib.check(_lib.load().tdz_tsurff_amplitudes(self.handle, _lib.dptr(out), C.c_void_p(s)))
         return out.view(np.complex128)
 
+    def interior(self, psi, stream=None) -> np.ndarray:
+        """Projection of psi inside |x_d| < R onto the Volkov states at the
+        last sample time (``Interior``, ``src/tsurff.cpp:565-639``): add it to
+        ``amplitudes()`` for the spectrum of a run that ends early."""
+        import torch
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        out = np.zeros(2 * int(np.prod(self.nk)))
+        _lib.check(_lib.load().tdz_tsurff_interior(self.handle, C.c_void_p(psi.data_ptr()), _lib.dptr(out),
+                                                   C.c_void_p(s)))
+        return out.view(np.complex128)
+
     def volkov(self):
         out = np.zeros(8)
         _lib.check(_lib.load().tdz_tsurff_volkov(self.handle, _lib.dptr(out)))

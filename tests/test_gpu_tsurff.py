@@ -41,12 +41,16 @@ def test_tsurff_parity(cuda, dim):
     assert np.abs(a - amp).max() <= 1e-11 * np.abs(amp).max()
     v = gpu.volkov()
     assert np.allclose(v[:3], ora.A) and np.allclose(v[3:6], ora.B) and abs(v[6] - ora.C) < 1e-12
+    # interior projection of the last state onto the Volkov states at the last sample
+    ki = gpu.interior(torch.tensor(psi, device=cuda))
+    kr = ora.interior(psi, [np.linspace(*k) for k in kg])
+    assert np.abs(ki - kr).max() <= 1e-11 * np.abs(kr).max(), np.abs(ki - kr).max() / np.abs(kr).max()
 
 
 @pytest.mark.gpu
 def test_tsurff_free_packet_gpu(cuda):
     """FREE1D deck of test_tsurff.py (p = 7, 400 elements, Pade(2,2), dt 0.025,
-    T = 20, R = 10): GPU propagation + GPU flux, plus the oracle's interior
+    T = 20, R = 10): GPU propagation, GPU flux and the GPU interior
     projection of psi(T), against the analytic spectrum at 1e-4."""
     import torch
     from tdsez_gb300.operators import Operator, Physics
@@ -63,10 +67,7 @@ def test_tsurff_free_packet_gpu(cuda):
     ts = TSurff(PS, 10.0, [(-1.0, 5.0, 61)], lambda t: [0.0, 0.0, 0.0], 0.025)
     G.evolve(psi, 0.025, 20.0, monitor=lambda step, t, ps: ts.sample(t, ps))
     amp = ts.amplitudes()
-    S = ob.Space([ob.Axis(kn, p, 10)])
-    ora = ots.OracleTSurff(S, 10.0, [np.linspace(-1, 5, 61)], 1.0, 0.0, 1.0, lambda t: [0, 0, 0], 0.025)
-    ora.advance_volkov(20.0)
-    tot = amp + ora.interior(psi.cpu().numpy(), [np.linspace(-1, 5, 61)])
+    tot = amp + ts.interior(psi)
     ks = np.linspace(-1, 5, 61)
     ex = (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ks - k0) ** 2)
     assert np.abs(np.abs(tot) ** 2 - ex).max() / ex.max() < 1e-4
