@@ -7,7 +7,9 @@
 // factorisation): the per-element tensor-contraction flops of this term.
 #include "quad.h"
 
+#include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "cplx.cuh"
 
@@ -181,6 +183,205 @@ __global__ void __launch_bounds__(kQThreads) k_quad(const QuadParams<T> prm) {
     }
 }
 
+// ---------------------------------------------------------------- streaming 3D kernel (FP32)
+// For axes whose elements own consecutive coefficient windows (no repeated
+// knots) and Q = p + 1 Gauss points. A CTA owns TE x TE elements in (x, y)
+// and streams a chunk of their z column. Interpolation of a coefficient plane
+// to the tile's (TE Q)^2 quadrature points (x, then y) is done once per
+// plane and kept in a ring of p + 1 planes; per z element every quadrature
+// column is interpolated along z, multiplied by w V (V from the closed form)
+// and projected back along z into a ring of p + 1 accumulator planes; a
+// coefficient plane whose elements are all done is projected back along y
+// and x and added to y with one atomic per coefficient and tile (the tiles
+// overlap by p coefficients per axis, chunk ends by p planes). Versus one CTA
+// per element: each interpolated plane serves p + 1 elements and the
+// coefficients receive (1 + p/TE)^2 atomic adds instead of (p+1)^3.
+template <int P, int TE> struct QStream {
+    static constexpr int NP = P + 1, Q = P + 1, TQ = TE * Q, TC = TE + P, PL = TQ * TQ;
+    static constexpr size_t smem = sizeof(float2) * ((size_t)2 * NP * PL + TC * TC + TC * TQ);
+};
+constexpr int kQsThreads = 512;
+// tile side in elements: the two rings of (TE (p+1))^2 points fit the 227 KB of shared memory
+template <int P> constexpr int qs_te() { return P <= 4 ? 8 : 6; }
+
+template <int P, int TE>
+__global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<float> prm, int zchunk) {
+    using S = QStream<P, TE>;
+    constexpr int NP = S::NP, Q = S::Q, TQ = S::TQ, TC = S::TC, PL = S::PL;
+    extern __shared__ float2 qs_raw[];
+    float2 *sV = qs_raw;               // [NP][PL] x,y-interpolated coefficient planes (ring, row qy, column qx)
+    float2 *sG = sV + NP * PL;         // [NP][PL] z-projected accumulators (ring)
+    float2 *sX = sG + NP * PL;         // [TC][TC] staged coefficient plane
+    float2 *sU = sX + TC * TC;         // [TC][TQ] x-interpolated rows, then the back-y rows
+    __shared__ float sNx[TE * Q * NP], sNy[TE * Q * NP], sNz[Q * NP];
+    __shared__ float sWx[TQ], sWy[TQ], sXx[TQ], sXy[TQ], sWz[Q], sXz[Q];
+    const int tid = threadIdx.x;
+    const int nelx = prm.nel[0], nely = prm.nel[1], nelz = prm.nel[2];
+    const int tilesX = (nelx + TE - 1) / TE;
+    const int ex0 = (blockIdx.x % tilesX) * TE, ey0 = (blockIdx.x / tilesX) * TE;
+    const int ez0 = blockIdx.y * zchunk, ez1 = min(nelz, ez0 + zchunk);
+    if (ez0 >= ez1) return;
+    const int n0 = prm.n[0], n1 = prm.n[1], n2 = prm.n[2];
+    const int cx0 = prm.off[0][ex0], cy0 = prm.off[1][ey0];
+    // per-tile tables (elements past the grid: zero rows, no contribution)
+    for (int i = tid; i < TE * Q * NP; i += kQsThreads) {
+        const int e = i / (Q * NP), r = i % (Q * NP);
+        sNx[i] = ex0 + e < nelx ? prm.N[0][(size_t)(ex0 + e) * Q * NP + r] : 0.f;
+        sNy[i] = ey0 + e < nely ? prm.N[1][(size_t)(ey0 + e) * Q * NP + r] : 0.f;
+    }
+    for (int i = tid; i < TQ; i += kQsThreads) {
+        const int e = i / Q;
+        const bool inx = ex0 + e < nelx, iny = ey0 + e < nely;
+        sWx[i] = inx ? prm.w[0][(size_t)ex0 * Q + i] : 0.f;
+        sXx[i] = inx ? prm.xq[0][(size_t)ex0 * Q + i] : 0.f;
+        sWy[i] = iny ? prm.w[1][(size_t)ey0 * Q + i] : 0.f;
+        sXy[i] = iny ? prm.xq[1][(size_t)ey0 * Q + i] : 0.f;
+    }
+    for (int i = tid; i < NP * PL; i += kQsThreads) sG[i] = make_float2(0.f, 0.f);
+    const float2 *X = static_cast<const float2 *>(prm.x);
+    float2 *Y = static_cast<float2 *>(prm.y);
+    __syncthreads();
+
+    // coefficient plane kz -> sV[kz % NP]
+    auto interpolate_plane = [&](int kz) {
+        for (int i = tid; i < TC * TC; i += kQsThreads) {
+            const int iy = i / TC, ix = i % TC, gy = cy0 + iy, gx = cx0 + ix;
+            sX[i] = (gy < n1 && gx < n0 && kz < n2) ? X[((size_t)kz * n1 + gy) * n0 + gx] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        for (int i = tid; i < TC * TQ; i += kQsThreads) {   // x: sU[iy][qx]
+            const int iy = i / TQ, qx = i % TQ, e = qx / Q;
+            const float *nx = sNx + qx * NP;
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < NP; ++c) rfma(a, nx[c], sX[iy * TC + e + c]);
+            sU[i] = a;
+        }
+        __syncthreads();
+        float2 *v = sV + (size_t)(kz % NP) * PL;
+        for (int i = tid; i < PL; i += kQsThreads) {        // y: v[qy][qx]
+            const int qy = i / TQ, qx = i % TQ, e = qy / Q;
+            const float *ny = sNy + qy * NP;
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < NP; ++c) rfma(a, ny[c], sU[(e + c) * TQ + qx]);
+            v[i] = a;
+        }
+        __syncthreads();
+    };
+    // complete coefficient plane kz in sG[kz % NP]: back along y and x, add to y, clear
+    const float cre = prm.cre, cim = prm.cim;
+    auto flush_plane = [&](int kz) {
+        float2 *g = sG + (size_t)(kz % NP) * PL;
+        for (int i = tid; i < TC * TQ; i += kQsThreads) {   // back y: sU[iy][qx]
+            const int iy = i / TQ, qx = i % TQ;
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < NP; ++c) {
+                const int e = iy - c;
+                if (e < 0 || e >= TE) continue;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) rfma(a, sNy[(e * Q + q) * NP + c], g[(e * Q + q) * TQ + qx]);
+            }
+            sU[i] = a;
+        }
+        __syncthreads();
+        for (int i = tid; i < TC * TC; i += kQsThreads) {   // back x, add to y
+            const int iy = i / TC, ix = i % TC, gy = cy0 + iy, gx = cx0 + ix;
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < NP; ++c) {
+                const int e = ix - c;
+                if (e < 0 || e >= TE) continue;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) rfma(a, sNx[(e * Q + q) * NP + c], sU[iy * TQ + e * Q + q]);
+            }
+            if (gy < n1 && gx < n0 && kz < n2 && (a.x != 0.f || a.y != 0.f)) {
+                float2 *dst = &Y[((size_t)kz * n1 + gy) * n0 + gx];
+                atomicAdd(&dst->x, cre * a.x - cim * a.y);
+                atomicAdd(&dst->y, cre * a.y + cim * a.x);
+            }
+        }
+        for (int i = tid; i < PL; i += kQsThreads) g[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+    };
+
+    const int cz0 = prm.off[2][ez0];
+    for (int c = 0; c < P; ++c) interpolate_plane(cz0 + c);
+    for (int ez = ez0; ez < ez1; ++ez) {
+        const int cz = prm.off[2][ez];
+        interpolate_plane(cz + P);
+        for (int i = tid; i < Q * NP; i += kQsThreads) sNz[i] = prm.N[2][(size_t)ez * Q * NP + i];
+        for (int i = tid; i < Q; i += kQsThreads) {
+            sWz[i] = prm.w[2][(size_t)ez * Q + i];
+            sXz[i] = prm.xq[2][(size_t)ez * Q + i];
+        }
+        __syncthreads();
+        // z: interpolate, times w V, project back, per quadrature column
+        for (int i = tid; i < PL; i += kQsThreads) {
+            const int qy = i / TQ, qx = i % TQ;
+            float2 v[NP], g[NP];
+#pragma unroll
+            for (int c = 0; c < NP; ++c) {
+                v[c] = sV[(size_t)((cz + c) % NP) * PL + i];
+                g[c] = make_float2(0.f, 0.f);
+            }
+            const float wxy = sWx[qx] * sWy[qy], x = sXx[qx], y = sXy[qy];
+#pragma unroll
+            for (int qz = 0; qz < Q; ++qz) {
+                float2 f = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int c = 0; c < NP; ++c) rfma(f, sNz[qz * NP + c], v[c]);
+                float pot = 0.f;
+                for (int k = 0; k < prm.nsoft; ++k) {
+                    const float dx = x - prm.soft[k][1], dy = y - prm.soft[k][2], dz = sXz[qz] - prm.soft[k][3];
+                    pot -= prm.soft[k][0] * rsqrtf(dx * dx + dy * dy + dz * dz + prm.soft[k][4]);
+                }
+                const float wv = wxy * sWz[qz] * pot;
+                f.x *= wv;
+                f.y *= wv;
+#pragma unroll
+                for (int c = 0; c < NP; ++c) rfma(g[c], sNz[qz * NP + c], f);
+            }
+#pragma unroll
+            for (int c = 0; c < NP; ++c) {
+                float2 &d = sG[(size_t)((cz + c) % NP) * PL + i];
+                d.x += g[c].x;
+                d.y += g[c].y;
+            }
+        }
+        __syncthreads();
+        flush_plane(cz);   // no later element of the chunk touches plane cz
+    }
+    // planes with contributions from the chunk's last elements
+    const int czl = prm.off[2][ez1 - 1];
+    for (int c = 1; c <= P; ++c) flush_plane(czl + c);
+}
+
+// the streaming kernel applies: 3D, FP32, Q = p + 1, consecutive element offsets on every axis
+bool stream_ok(const QuadTerm &q, int prec) {
+    if (q.dim != 3 || prec != TDZ_FP32 || q.nq != q.p + 1) return false;
+    return q.consecutive;
+}
+
+template <int P>
+void launch_q3s(const QuadTerm &q, const QuadParams<float> &prm, cudaStream_t st) {
+    constexpr int TE = qs_te<P>();
+    using S = QStream<P, TE>;
+    auto kern = k_quad3_stream<P, TE>;
+    static const bool attr = [&] {
+        TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem));
+        return true;
+    }();
+    (void)attr;
+    const int tiles = ((q.nel[0] + TE - 1) / TE) * ((q.nel[1] + TE - 1) / TE);
+    // about two CTAs per SM in total, z chunks no shorter than 4 (p + 1) elements
+    int chunks = std::max(1, (2 * sm_count() + tiles - 1) / tiles);
+    chunks = std::max(1, std::min(chunks, q.nel[2] / (4 * (P + 1))));
+    const int zchunk = (q.nel[2] + chunks - 1) / chunks;
+    kern<<<dim3(tiles, (q.nel[2] + zchunk - 1) / zchunk), kQsThreads, S::smem, st>>>(prm, zchunk);
+}
+
 template <class T>
 QuadParams<T> make_qparams(const QuadTerm &q, cd coef, const void *x, void *y) {
     QuadParams<T> prm{};
@@ -217,6 +418,17 @@ void launch_q(const QuadTerm &q, const QuadParams<T> &prm, cudaStream_t st) {
 template <class T>
 void dispatch_q(const QuadTerm &q, cd coef, const void *x, void *y, cudaStream_t st) {
     const QuadParams<T> prm = make_qparams<T>(q, coef, x, y);
+    if constexpr (std::is_same<T, float>::value) {
+        if (stream_ok(q, TDZ_FP32)) {
+            switch (q.p) {
+            case 2: launch_q3s<2>(q, prm, st); return;
+            case 3: launch_q3s<3>(q, prm, st); return;
+            case 4: launch_q3s<4>(q, prm, st); return;
+            case 5: launch_q3s<5>(q, prm, st); return;
+            default: break;
+            }
+        }
+    }
     switch (q.p) {
     case 2: launch_q<T, 2>(q, prm, st); break;
     case 3: launch_q<T, 3>(q, prm, st); break;
@@ -243,9 +455,12 @@ void QuadTerm::build(const Space &s, int nsoft_, const double *soft_) {
     dim = s.dim;
     p = s.ax[0].p;
     nq = s.nquad;
+    consecutive = true;
     for (int d = 0; d < dim; ++d) {
         const Axis1D &a = s.ax[d];
         TDZ_CHECK(a.nq == nq && a.p == p, TDZ_ERR_INTERNAL, "axis tables disagree");
+        for (int e = 0; e + 1 < a.nel; ++e)
+            if (a.offset[e + 1] != a.offset[e] + 1) consecutive = false;
         nel[d] = a.nel;
         n[d] = a.n;
         std::vector<int> o(a.offset.begin(), a.offset.end());

@@ -23,6 +23,7 @@ struct QuadTerm {
     double soft[kMaxSoft][5] = {};    // Z, cx, cy, cz, a
     int dim = 0, p = 0, nq = 0;
     int nel[3] = {1, 1, 1}, n[3] = {1, 1, 1};
+    bool consecutive = false;         // every element's window starts one coefficient after the last one's
     // per axis: first basis index per element, basis values [e][q][a], weights [e][q], points [e][q]
     DevBuf off[3], N32[3], N64[3], w64[3], x64[3], w32[3], x32[3];
     void build(const Space &s, int nsoft_, const double *soft_);

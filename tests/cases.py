@@ -138,6 +138,18 @@ def _c10():
                 soft=[(0.5, -1.0, 0.0, 0.0, 1.0), (0.7, 1.0, 0.5, -0.5, 0.8)])
 
 
+@case("3d_softcore_tiles")
+def _c11():
+    """Two soft-core centres on a grid of several element tiles in x and y
+    and two chunks along z (the tiled, z-streamed quadrature kernel), graded
+    knots on x and z, p = 3."""
+    p, nq = 3, 4
+    knots = [ob.symexp_knots(-20.0, 20.0, 15, 0.9, p), ob.uniform_knots(12, -18.0, 18.0, p),
+             ob.symexp_knots(-24.0, 24.0, 43, 0.9, p)]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, coupled=(2,),
+                soft=[(1.0, 0.3, -0.2, 0.1, 0.5), (0.5, -2.0, 1.0, 3.0, 1.0)])
+
+
 def _soft_value(soft, r):
     v = 0.0
     for Z, cx, cy, cz, a in soft:
