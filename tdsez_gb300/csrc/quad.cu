@@ -29,6 +29,7 @@ template <class T> struct QuadParams {
     int nsoft;
     T soft[kMaxSoft][5];
     T cre, cim;
+    double cre_d, cim_d;
 };
 
 __device__ __forceinline__ void atomic_add_c(float2 *p, float2 v) {
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(kQThreads) k_quad(const QuadParams<T> prm) {
     }
 }
 
-// ---------------------------------------------------------------- streaming 3D kernel (FP32)
+// ---------------------------------------------------------------- streaming 3D kernel
 // For axes whose elements own consecutive coefficient windows (no repeated
 // knots) and Q = p + 1 Gauss points. A CTA owns TE x TE elements in (x, y)
 // and streams a chunk of their z column. Interpolation of a coefficient plane
@@ -196,25 +197,92 @@ __global__ void __launch_bounds__(kQThreads) k_quad(const QuadParams<T> prm) {
 // overlap by p coefficients per axis, chunk ends by p planes). Versus one CTA
 // per element: each interpolated plane serves p + 1 elements and the
 // coefficients receive (1 + p/TE)^2 atomic adds instead of (p+1)^3.
-template <int P, int TE> struct QStream {
+// FP32 arithmetic on FP32 vectors, or double-float arithmetic on FP64
+// vectors (the FGMRES applies: 1/sqrt of the potential by rsqrtf and one
+// Newton step in double-float, about 48 bits).
+template <class A> struct QArith;
+template <> struct QArith<float> {
+    using C = float2;
+    using MC = float2;
+    using TT = float;
+    __device__ static float from(TT v) { return v; }
+    __device__ static float one() { return 1.f; }
+    // -Z / sqrt(r2 + a) summed over the centres at (x, y, z)
+    __device__ static float pot(const QuadParams<TT> &prm, float x, float y, float z) {
+        float v = 0.f;
+        for (int k = 0; k < prm.nsoft; ++k) {
+            const float dx = x - prm.soft[k][1], dy = y - prm.soft[k][2], dz = z - prm.soft[k][3];
+            v -= prm.soft[k][0] * rsqrtf(dx * dx + dy * dy + dz * dz + prm.soft[k][4]);
+        }
+        return v;
+    }
+    __device__ static float mul(float a, float b) { return a * b; }
+    __device__ static void scale(float2 &f, float w) { f.x *= w; f.y *= w; }
+    __device__ static void atomic_out(float2 *dst, float2 a, double cre, double cim) {
+        atomicAdd(&dst->x, (float)cre * a.x - (float)cim * a.y);
+        atomicAdd(&dst->y, (float)cre * a.y + (float)cim * a.x);
+    }
+};
+template <> struct QArith<dff> {
+    using C = cdff;
+    using MC = double2;
+    using TT = double;
+    __device__ static dff from(TT v) { return dff_split(v); }
+    __device__ static dff one() { return dff(1.f); }
+    __device__ static dff mul(dff a, dff b) { return renorm(tfma(a, b, dff(0.f))); }
+    __device__ static dff pot(const QuadParams<TT> &prm, dff x, dff y, dff z) {
+        dff v(0.f);
+        for (int k = 0; k < prm.nsoft; ++k) {
+            const dff dx = renorm(tfma(dff(1.f), x, dff_split(-prm.soft[k][1])));
+            const dff dy = renorm(tfma(dff(1.f), y, dff_split(-prm.soft[k][2])));
+            const dff dz = renorm(tfma(dff(1.f), z, dff_split(-prm.soft[k][3])));
+            const dff r2 = renorm(tfma(dx, dx, tfma(dy, dy, tfma(dz, dz, dff_split(prm.soft[k][4])))));
+            // 1/sqrt(r2): rsqrtf, then one Newton step y1 = y0 - y0 (r2 y0^2 - 1) / 2 in double-float
+            const float y0 = rsqrtf(r2.hi);
+            const dff t = renorm(tfma(dff(y0), dff(y0), dff(0.f)));            // y0^2, exact
+            const dff u = renorm(tfma(r2, t, dff(-1.f)));                       // r2 y0^2 - 1
+            const dff yi = renorm(tfma(dff(-0.5f * y0), u, dff(y0)));
+            v = renorm(tfma(dff_split(-prm.soft[k][0]), yi, v));
+        }
+        return v;
+    }
+    __device__ static void scale(cdff &f, dff w) {
+        f.x = renorm(tfma(f.x, w, dff(0.f)));
+        f.y = renorm(tfma(f.y, w, dff(0.f)));
+    }
+    __device__ static void atomic_out(double2 *dst, cdff a, double cre, double cim) {
+        const double ax = dff_to_double(a.x), ay = dff_to_double(a.y);
+        atomicAdd(&dst->x, cre * ax - cim * ay);
+        atomicAdd(&dst->y, cre * ay + cim * ax);
+    }
+};
+
+template <class A, int P, int TE> struct QStream {
+    using C = typename QArith<A>::C;
     static constexpr int NP = P + 1, Q = P + 1, TQ = TE * Q, TC = TE + P, PL = TQ * TQ;
-    static constexpr size_t smem = sizeof(float2) * ((size_t)2 * NP * PL + TC * TC + TC * TQ);
+    static constexpr size_t smem = sizeof(C) * ((size_t)2 * NP * PL + TC * TC + TC * TQ);
 };
 constexpr int kQsThreads = 512;
 // tile side in elements: the two rings of (TE (p+1))^2 points fit the 227 KB of shared memory
-template <int P> constexpr int qs_te() { return P <= 4 ? 8 : 6; }
+template <class A, int P> constexpr int qs_te() {
+    return std::is_same<A, float>::value ? (P <= 4 ? 8 : 6) : (P <= 3 ? 7 : (P == 4 ? 6 : 4));
+}
 
-template <int P, int TE>
-__global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<float> prm, int zchunk) {
-    using S = QStream<P, TE>;
+template <class A, int P, int TE>
+__global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<typename QArith<A>::TT> prm,
+                                                             int zchunk) {
+    using Q3 = QArith<A>;
+    using C = typename Q3::C;
+    using MC = typename Q3::MC;
+    using S = QStream<A, P, TE>;
     constexpr int NP = S::NP, Q = S::Q, TQ = S::TQ, TC = S::TC, PL = S::PL;
-    extern __shared__ float2 qs_raw[];
-    float2 *sV = qs_raw;               // [NP][PL] x,y-interpolated coefficient planes (ring, row qy, column qx)
-    float2 *sG = sV + NP * PL;         // [NP][PL] z-projected accumulators (ring)
-    float2 *sX = sG + NP * PL;         // [TC][TC] staged coefficient plane
-    float2 *sU = sX + TC * TC;         // [TC][TQ] x-interpolated rows, then the back-y rows
-    __shared__ float sNx[TE * Q * NP], sNy[TE * Q * NP], sNz[Q * NP];
-    __shared__ float sWx[TQ], sWy[TQ], sXx[TQ], sXy[TQ], sWz[Q], sXz[Q];
+    extern __shared__ __align__(16) unsigned char qs_raw[];
+    C *sV = reinterpret_cast<C *>(qs_raw);   // [NP][PL] x,y-interpolated coefficient planes (ring, row qy, column qx)
+    C *sG = sV + NP * PL;                    // [NP][PL] z-projected accumulators (ring)
+    C *sX = sG + NP * PL;                    // [TC][TC] staged coefficient plane
+    C *sU = sX + TC * TC;                    // [TC][TQ] x-interpolated rows, then the back-y rows
+    __shared__ A sNx[TE * Q * NP], sNy[TE * Q * NP], sNz[Q * NP];
+    __shared__ A sWx[TQ], sWy[TQ], sXx[TQ], sXy[TQ], sWz[Q], sXz[Q];
     const int tid = threadIdx.x;
     const int nelx = prm.nel[0], nely = prm.nel[1], nelz = prm.nel[2];
     const int tilesX = (nelx + TE - 1) / TE;
@@ -223,59 +291,59 @@ __global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<fl
     if (ez0 >= ez1) return;
     const int n0 = prm.n[0], n1 = prm.n[1], n2 = prm.n[2];
     const int cx0 = prm.off[0][ex0], cy0 = prm.off[1][ey0];
+    const A zero = A(0.f);
     // per-tile tables (elements past the grid: zero rows, no contribution)
     for (int i = tid; i < TE * Q * NP; i += kQsThreads) {
         const int e = i / (Q * NP), r = i % (Q * NP);
-        sNx[i] = ex0 + e < nelx ? prm.N[0][(size_t)(ex0 + e) * Q * NP + r] : 0.f;
-        sNy[i] = ey0 + e < nely ? prm.N[1][(size_t)(ey0 + e) * Q * NP + r] : 0.f;
+        sNx[i] = ex0 + e < nelx ? Q3::from(prm.N[0][(size_t)(ex0 + e) * Q * NP + r]) : zero;
+        sNy[i] = ey0 + e < nely ? Q3::from(prm.N[1][(size_t)(ey0 + e) * Q * NP + r]) : zero;
     }
     for (int i = tid; i < TQ; i += kQsThreads) {
         const int e = i / Q;
         const bool inx = ex0 + e < nelx, iny = ey0 + e < nely;
-        sWx[i] = inx ? prm.w[0][(size_t)ex0 * Q + i] : 0.f;
-        sXx[i] = inx ? prm.xq[0][(size_t)ex0 * Q + i] : 0.f;
-        sWy[i] = iny ? prm.w[1][(size_t)ey0 * Q + i] : 0.f;
-        sXy[i] = iny ? prm.xq[1][(size_t)ey0 * Q + i] : 0.f;
+        sWx[i] = inx ? Q3::from(prm.w[0][(size_t)ex0 * Q + i]) : zero;
+        sXx[i] = inx ? Q3::from(prm.xq[0][(size_t)ex0 * Q + i]) : zero;
+        sWy[i] = iny ? Q3::from(prm.w[1][(size_t)ey0 * Q + i]) : zero;
+        sXy[i] = iny ? Q3::from(prm.xq[1][(size_t)ey0 * Q + i]) : zero;
     }
-    for (int i = tid; i < NP * PL; i += kQsThreads) sG[i] = make_float2(0.f, 0.f);
-    const float2 *X = static_cast<const float2 *>(prm.x);
-    float2 *Y = static_cast<float2 *>(prm.y);
+    for (int i = tid; i < NP * PL; i += kQsThreads) sG[i] = czero<C>();
+    const MC *X = static_cast<const MC *>(prm.x);
+    MC *Y = static_cast<MC *>(prm.y);
     __syncthreads();
 
     // coefficient plane kz -> sV[kz % NP]
     auto interpolate_plane = [&](int kz) {
         for (int i = tid; i < TC * TC; i += kQsThreads) {
             const int iy = i / TC, ix = i % TC, gy = cy0 + iy, gx = cx0 + ix;
-            sX[i] = (gy < n1 && gx < n0 && kz < n2) ? X[((size_t)kz * n1 + gy) * n0 + gx] : make_float2(0.f, 0.f);
+            sX[i] = (gy < n1 && gx < n0 && kz < n2) ? load_c<C, MC>(X[((size_t)kz * n1 + gy) * n0 + gx]) : czero<C>();
         }
         __syncthreads();
         for (int i = tid; i < TC * TQ; i += kQsThreads) {   // x: sU[iy][qx]
             const int iy = i / TQ, qx = i % TQ, e = qx / Q;
-            const float *nx = sNx + qx * NP;
-            float2 a = make_float2(0.f, 0.f);
+            const A *nx = sNx + qx * NP;
+            C a = czero<C>();
 #pragma unroll
             for (int c = 0; c < NP; ++c) rfma(a, nx[c], sX[iy * TC + e + c]);
-            sU[i] = a;
+            sU[i] = cnorm(a);
         }
         __syncthreads();
-        float2 *v = sV + (size_t)(kz % NP) * PL;
+        C *v = sV + (size_t)(kz % NP) * PL;
         for (int i = tid; i < PL; i += kQsThreads) {        // y: v[qy][qx]
             const int qy = i / TQ, qx = i % TQ, e = qy / Q;
-            const float *ny = sNy + qy * NP;
-            float2 a = make_float2(0.f, 0.f);
+            const A *ny = sNy + qy * NP;
+            C a = czero<C>();
 #pragma unroll
             for (int c = 0; c < NP; ++c) rfma(a, ny[c], sU[(e + c) * TQ + qx]);
-            v[i] = a;
+            v[i] = cnorm(a);
         }
         __syncthreads();
     };
     // complete coefficient plane kz in sG[kz % NP]: back along y and x, add to y, clear
-    const float cre = prm.cre, cim = prm.cim;
     auto flush_plane = [&](int kz) {
-        float2 *g = sG + (size_t)(kz % NP) * PL;
+        C *g = sG + (size_t)(kz % NP) * PL;
         for (int i = tid; i < TC * TQ; i += kQsThreads) {   // back y: sU[iy][qx]
             const int iy = i / TQ, qx = i % TQ;
-            float2 a = make_float2(0.f, 0.f);
+            C a = czero<C>();
 #pragma unroll
             for (int c = 0; c < NP; ++c) {
                 const int e = iy - c;
@@ -283,12 +351,12 @@ __global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<fl
 #pragma unroll
                 for (int q = 0; q < Q; ++q) rfma(a, sNy[(e * Q + q) * NP + c], g[(e * Q + q) * TQ + qx]);
             }
-            sU[i] = a;
+            sU[i] = cnorm(a);
         }
         __syncthreads();
         for (int i = tid; i < TC * TC; i += kQsThreads) {   // back x, add to y
             const int iy = i / TC, ix = i % TC, gy = cy0 + iy, gx = cx0 + ix;
-            float2 a = make_float2(0.f, 0.f);
+            C a = czero<C>();
 #pragma unroll
             for (int c = 0; c < NP; ++c) {
                 const int e = ix - c;
@@ -296,13 +364,10 @@ __global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<fl
 #pragma unroll
                 for (int q = 0; q < Q; ++q) rfma(a, sNx[(e * Q + q) * NP + c], sU[iy * TQ + e * Q + q]);
             }
-            if (gy < n1 && gx < n0 && kz < n2 && (a.x != 0.f || a.y != 0.f)) {
-                float2 *dst = &Y[((size_t)kz * n1 + gy) * n0 + gx];
-                atomicAdd(&dst->x, cre * a.x - cim * a.y);
-                atomicAdd(&dst->y, cre * a.y + cim * a.x);
-            }
+            if (gy < n1 && gx < n0 && kz < n2)
+                Q3::atomic_out(&Y[((size_t)kz * n1 + gy) * n0 + gx], cnorm(a), prm.cre_d, prm.cim_d);
         }
-        for (int i = tid; i < PL; i += kQsThreads) g[i] = make_float2(0.f, 0.f);
+        for (int i = tid; i < PL; i += kQsThreads) g[i] = czero<C>();
         __syncthreads();
     };
 
@@ -311,43 +376,38 @@ __global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<fl
     for (int ez = ez0; ez < ez1; ++ez) {
         const int cz = prm.off[2][ez];
         interpolate_plane(cz + P);
-        for (int i = tid; i < Q * NP; i += kQsThreads) sNz[i] = prm.N[2][(size_t)ez * Q * NP + i];
+        for (int i = tid; i < Q * NP; i += kQsThreads) sNz[i] = Q3::from(prm.N[2][(size_t)ez * Q * NP + i]);
         for (int i = tid; i < Q; i += kQsThreads) {
-            sWz[i] = prm.w[2][(size_t)ez * Q + i];
-            sXz[i] = prm.xq[2][(size_t)ez * Q + i];
+            sWz[i] = Q3::from(prm.w[2][(size_t)ez * Q + i]);
+            sXz[i] = Q3::from(prm.xq[2][(size_t)ez * Q + i]);
         }
         __syncthreads();
         // z: interpolate, times w V, project back, per quadrature column
         for (int i = tid; i < PL; i += kQsThreads) {
             const int qy = i / TQ, qx = i % TQ;
-            float2 v[NP], g[NP];
+            C v[NP], g[NP];
 #pragma unroll
             for (int c = 0; c < NP; ++c) {
                 v[c] = sV[(size_t)((cz + c) % NP) * PL + i];
-                g[c] = make_float2(0.f, 0.f);
+                g[c] = czero<C>();
             }
-            const float wxy = sWx[qx] * sWy[qy], x = sXx[qx], y = sXy[qy];
+            const A wxy = Q3::mul(sWx[qx], sWy[qy]);
 #pragma unroll
             for (int qz = 0; qz < Q; ++qz) {
-                float2 f = make_float2(0.f, 0.f);
+                C f = czero<C>();
 #pragma unroll
                 for (int c = 0; c < NP; ++c) rfma(f, sNz[qz * NP + c], v[c]);
-                float pot = 0.f;
-                for (int k = 0; k < prm.nsoft; ++k) {
-                    const float dx = x - prm.soft[k][1], dy = y - prm.soft[k][2], dz = sXz[qz] - prm.soft[k][3];
-                    pot -= prm.soft[k][0] * rsqrtf(dx * dx + dy * dy + dz * dz + prm.soft[k][4]);
-                }
-                const float wv = wxy * sWz[qz] * pot;
-                f.x *= wv;
-                f.y *= wv;
+                f = cnorm(f);
+                const A wv = Q3::mul(Q3::mul(wxy, sWz[qz]), Q3::pot(prm, sXx[qx], sXy[qy], sXz[qz]));
+                Q3::scale(f, wv);
 #pragma unroll
                 for (int c = 0; c < NP; ++c) rfma(g[c], sNz[qz * NP + c], f);
             }
 #pragma unroll
             for (int c = 0; c < NP; ++c) {
-                float2 &d = sG[(size_t)((cz + c) % NP) * PL + i];
-                d.x += g[c].x;
-                d.y += g[c].y;
+                C &d = sG[(size_t)((cz + c) % NP) * PL + i];
+                rfma(d, Q3::one(), cnorm(g[c]));
+                d = cnorm(d);
             }
         }
         __syncthreads();
@@ -358,17 +418,15 @@ __global__ void __launch_bounds__(kQsThreads) k_quad3_stream(const QuadParams<fl
     for (int c = 1; c <= P; ++c) flush_plane(czl + c);
 }
 
-// the streaming kernel applies: 3D, FP32, Q = p + 1, consecutive element offsets on every axis
-bool stream_ok(const QuadTerm &q, int prec) {
-    if (q.dim != 3 || prec != TDZ_FP32 || q.nq != q.p + 1) return false;
-    return q.consecutive;
-}
+// the streaming kernel applies: 3D, Q = p + 1, consecutive element offsets on every axis
+bool stream_ok(const QuadTerm &q) { return q.dim == 3 && q.nq == q.p + 1 && q.consecutive; }
 
-template <int P>
-void launch_q3s(const QuadTerm &q, const QuadParams<float> &prm, cudaStream_t st) {
-    constexpr int TE = qs_te<P>();
-    using S = QStream<P, TE>;
-    auto kern = k_quad3_stream<P, TE>;
+template <class A, int P>
+void launch_q3s(const QuadTerm &q, const QuadParams<typename QArith<A>::TT> &prm, cudaStream_t st) {
+    constexpr int TE = qs_te<A, P>();
+    using S = QStream<A, P, TE>;
+    auto kern = k_quad3_stream<A, P, TE>;
+    static_assert(S::smem <= 200 * 1024, "quadrature rings larger than the shared memory");
     static const bool attr = [&] {
         TDZ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem));
         return true;
@@ -404,6 +462,8 @@ QuadParams<T> make_qparams(const QuadTerm &q, cd coef, const void *x, void *y) {
         for (int k = 0; k < 5; ++k) prm.soft[c][k] = (T)q.soft[c][k];
     prm.cre = (T)coef.real();
     prm.cim = (T)coef.imag();
+    prm.cre_d = coef.real();
+    prm.cim_d = coef.imag();
     return prm;
 }
 
@@ -418,15 +478,14 @@ void launch_q(const QuadTerm &q, const QuadParams<T> &prm, cudaStream_t st) {
 template <class T>
 void dispatch_q(const QuadTerm &q, cd coef, const void *x, void *y, cudaStream_t st) {
     const QuadParams<T> prm = make_qparams<T>(q, coef, x, y);
-    if constexpr (std::is_same<T, float>::value) {
-        if (stream_ok(q, TDZ_FP32)) {
-            switch (q.p) {
-            case 2: launch_q3s<2>(q, prm, st); return;
-            case 3: launch_q3s<3>(q, prm, st); return;
-            case 4: launch_q3s<4>(q, prm, st); return;
-            case 5: launch_q3s<5>(q, prm, st); return;
-            default: break;
-            }
+    if (stream_ok(q)) {   // FP32: FP32 arithmetic; FP64 vectors: double-float arithmetic
+        using A = typename std::conditional<std::is_same<T, float>::value, float, dff>::type;
+        switch (q.p) {
+        case 2: launch_q3s<A, 2>(q, prm, st); return;
+        case 3: launch_q3s<A, 3>(q, prm, st); return;
+        case 4: launch_q3s<A, 4>(q, prm, st); return;
+        case 5: launch_q3s<A, 5>(q, prm, st); return;
+        default: break;
         }
     }
     switch (q.p) {
