@@ -306,6 +306,13 @@ def run_tdz(args):
 
     mixed_mg = run_arm("fp32", args.mg_steps, outer=args.outer, **mg) if args.mg_steps > 0 else None
 
+    # ---- learned arm: FP32 multigrid with the learned coarse correction, its
+    # network trained on the coarse right-hand sides of the run's own first
+    # steps, beside the same hierarchy without the network
+    learned = None
+    if args.learned_steps > 0:
+        learned = learned_arms(args, op, psi0, w, stream)
+
     # ---- plain GPU multigrid arm (FP64 throughout)
     plain = run_arm("fp64", args.plain_steps, **mg) if args.plain_steps > 0 else None
 
@@ -350,6 +357,8 @@ def run_tdz(args):
         "vs_plain_mg": (value / plain["steps_per_s"]) if plain else None,
         "mixed_mg": mixed_mg,
         "plain_mg": plain,
+        "learned_mg": learned["learned"] if learned else None,
+        "mixed_mg_same_levels": learned["plain"] if learned else None,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N,
                 "steps": ke},
         "gpu_launches": int(launches),
@@ -387,6 +396,46 @@ CPU_GRID = (16, 16, 32)
 # profiles/k_apply3d_df_stage_heterostructure_160x160x320_p3.md). The narrow tiles re-read
 # their x / y halos, which the FP32-pipe-bound kernel can afford.
 DF_APPLY_TRAFFIC = 297.75e6 + 125.24e6
+
+
+def learned_arms(args, op, psi0, w, stream):
+    """CN steps with the FP32 multigrid (args.learned_levels levels, default
+    coarse polynomial) in FP64 FGMRES, with and without the learned coarse
+    correction. The network's training inputs are the coarsest right-hand
+    sides of the V-cycles of the learned arm's own first
+    args.learned_train_steps steps (untimed), then args.learned_steps steps are
+    timed after args.warmup more; the plain arm takes the same steps."""
+    import torch
+    from tdsez_gb300.propagator import Propagator
+    dt = w.dt
+    kw = dict(pc="mg", precision="fp32", outer=args.outer, rtol=args.rtol, mg_smooth=args.mg_smooth,
+              mg_coarse_its=args.mg_coarse_its, mg_levels=args.learned_levels)
+    out = {}
+    G = Propagator(op, "cn", field=w.field, mg_learned=True, **kw)
+    psi = psi0.clone()
+    t = 0.0
+    G.record_coarse(args.learned_pairs)
+    t0 = time.time()
+    for _ in range(args.learned_train_steps):
+        G.step(psi, t, dt)
+        t += dt
+    G.record_coarse(0)
+    loss, pairs = G.train_coarse(epochs=args.learned_epochs, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    t_start = t
+    psi_start = psi.clone()
+    sps, its, _ = _timed_steps(G, psi, t_start, dt, args.warmup, args.learned_steps, stream)
+    out["learned"] = {"steps_per_s": sps, "its_per_step": its, "levels": args.learned_levels,
+                      "train_pairs": pairs, "train_loss": loss, "train_steps": args.learned_train_steps,
+                      "train_epochs": args.learned_epochs, "train_s": train_s, "steps": args.learned_steps,
+                      "what": "FP32 multigrid with the CNN coarse correction (BF16 weights) in FP64 FGMRES"}
+    G0 = Propagator(op, "cn", field=w.field, **kw)
+    psi = psi_start.clone()
+    sps0, its0, _ = _timed_steps(G0, psi, t_start, dt, args.warmup, args.learned_steps, stream)
+    out["plain"] = {"steps_per_s": sps0, "its_per_step": its0, "levels": args.learned_levels,
+                    "steps": args.learned_steps, "what": "the same hierarchy without the network"}
+    return out
 
 
 def true_residual(G, op, psi, t, dt, w):
@@ -601,6 +650,11 @@ def main():
     ap.add_argument("--mg-smooth", type=int, default=8)
     ap.add_argument("--mg-coarse-its", type=int, default=12)
     ap.add_argument("--mg-levels", type=int, default=0)
+    ap.add_argument("--learned-steps", type=int, default=10, help="timed steps of the learned arm (0: skip it)")
+    ap.add_argument("--learned-levels", type=int, default=3)
+    ap.add_argument("--learned-train-steps", type=int, default=6)
+    ap.add_argument("--learned-pairs", type=int, default=64)
+    ap.add_argument("--learned-epochs", type=int, default=40)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="cfg5", choices=["cfg5", "cfg2", "cfg3"],

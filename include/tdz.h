@@ -329,6 +329,18 @@ tdz_status tdz_prop_step_batch(int count, tdz_prop *const *props, void *const *p
  * solver, multigrid cycles; last solve's iterations and relative residual. */
 tdz_status tdz_prop_stats(const tdz_prop *p, long long *solves, long long *its, long long *applies,
                           long long *cycles, int *last_its, double *last_rres);
+/* Learned coarse correction trained on the propagation itself (propagators
+ * created with TDZ_PC_MG, FP32 levels and mg_learned = 1): record_coarse
+ * makes each stage solver's V-cycles store the coarsest-level right-hand side
+ * of their next `capacity` cycles (0 stops recording); the steps taken
+ * meanwhile are ordinary steps. train_coarse then builds the training pairs
+ * from the recorded right-hand sides (production coarse solve, its residual,
+ * a 10x longer solve for the error, as tdz_solver_train_coarse) and trains
+ * each solver's network; *loss: the largest mean relative loss of the last
+ * epoch, *pairs: the pairs used. No counterpart in the reference. */
+tdz_status tdz_prop_record_coarse(tdz_prop *p, int capacity);
+tdz_status tdz_prop_train_coarse(tdz_prop *p, int epochs, float lr, unsigned long long seed, float *loss,
+                                 int *pairs, void *stream);
 /* Preconditioner rebuilds the refresh rule asked for (tdz_pc_refresh_stale
  * over the stage solves of this propagator). */
 tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds);

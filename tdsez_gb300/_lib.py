@@ -130,6 +130,8 @@ SIGNATURES = {
     "tdz_set_apply3d_shape": (None, [I, I]),
     "tdz_eigen_solve": (I, [VP, I, D, D, I, C.c_void_p, VP, C.POINTER(D), C.POINTER(D), C.POINTER(I), VP]),
     "tdz_prop_refreshes": (I, [VP, C.POINTER(LL)]),
+    "tdz_prop_record_coarse": (I, [VP, I]),
+    "tdz_prop_train_coarse": (I, [VP, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), C.POINTER(I), VP]),
     "tdz_pc_refresh_stale": (I, [C.POINTER(tdz_pc_refresh), I]),
     "tdz_strong_field_ratio": (I, [VP, I, D, D, FIELD_FN, VP, C.POINTER(D)]),
     "tdz_prop_step_batch": (I, [I, C.POINTER(VP), C.POINTER(VP), C.c_double, C.POINTER(C.POINTER(C.c_double)),

@@ -483,6 +483,39 @@ tdz_status tdz_eigen_solve(tdz_op *op, int nev, double target, double tol, int m
     });
 }
 
+static std::vector<tdz::Multigrid *> prop_learned_mgs(tdz_prop *p) {
+    TDZ_CHECK(p, TDZ_ERR_ARG, "null propagator");
+    std::vector<tdz::Multigrid *> out;
+    for (int k = 0; k < p->p.nsolvers; ++k) {
+        TDZ_CHECK(p->p.solver[k].opt.pc == TDZ_PC_MG, TDZ_ERR_STATE, "the learned coarse correction needs TDZ_PC_MG");
+        auto *mg = static_cast<tdz::Multigrid *>(p->p.solver[k].pc.get());
+        TDZ_CHECK(mg->lrn.on, TDZ_ERR_STATE, "propagator created without mg_learned (or with FP64 levels)");
+        out.push_back(mg);
+    }
+    return out;
+}
+
+tdz_status tdz_prop_record_coarse(tdz_prop *p, int capacity) {
+    return guarded([&] {
+        for (tdz::Multigrid *mg : prop_learned_mgs(p)) mg->record_coarse(capacity);
+    });
+}
+
+tdz_status tdz_prop_train_coarse(tdz_prop *p, int epochs, float lr, unsigned long long seed, float *loss,
+                                 int *pairs, void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(lr > 0.f && std::isfinite(lr) && epochs >= 1, TDZ_ERR_ARG, "bad epochs or learning rate");
+        float l = 0.f;
+        int np = 0;
+        for (tdz::Multigrid *mg : prop_learned_mgs(p)) {
+            np += mg->lrn.rec_n;
+            l = std::max(l, mg->train_recorded(epochs, lr, seed, static_cast<cudaStream_t>(stream)));
+        }
+        if (loss) *loss = l;
+        if (pairs) *pairs = np;
+    });
+}
+
 tdz_status tdz_prop_refreshes(const tdz_prop *p, long long *rebuilds) {
     return guarded([&] {
         TDZ_CHECK(p && rebuilds, TDZ_ERR_ARG, "null argument");

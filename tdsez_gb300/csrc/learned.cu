@@ -112,6 +112,26 @@ void Multigrid::coarse_correct(MGLevel &m, cudaStream_t st) {
     count_launch(3);
 }
 
+void Multigrid::record_coarse(int capacity) {
+    TDZ_CHECK(lrn.on, TDZ_ERR_STATE, "the learned coarse correction needs mg_learned and FP32 levels");
+    TDZ_CHECK(capacity >= 0, TDZ_ERR_ARG, "negative capacity");
+    if (capacity == 0) { lrn.rec_cap = lrn.rec_n; return; }
+    lrn.rec.alloc((size_t)capacity * lv.back().ndof * sizeof(float2));
+    lrn.rec_cap = capacity;
+    lrn.rec_n = 0;
+}
+
+float Multigrid::train_recorded(int epochs, float lr, uint64_t seed, cudaStream_t st) {
+    TDZ_CHECK(lrn.on, TDZ_ERR_STATE, "the learned coarse correction needs mg_learned and FP32 levels");
+    TDZ_CHECK(lrn.rec_n >= lrn.batch, TDZ_ERR_STATE,
+              "fewer recorded coarse right-hand sides than one training batch (record_coarse, then run steps)");
+    const int pairs = lrn.rec_n / lrn.batch * lrn.batch;
+    lrn.use_recorded = true;
+    const float l = train_coarse(pairs, epochs, lr, seed, st);
+    lrn.use_recorded = false;
+    return l;
+}
+
 float Multigrid::train_coarse(int pairs, int epochs, float lr, uint64_t seed, cudaStream_t st) {
     TDZ_CHECK(lrn.on, TDZ_ERR_STATE, "the learned coarse correction needs mg_learned and FP32 levels");
     TDZ_CHECK(pairs >= lrn.batch && epochs >= 1, TDZ_ERR_ARG, "need at least one batch of pairs and one epoch");
@@ -129,7 +149,10 @@ float Multigrid::train_coarse(int pairs, int epochs, float lr, uint64_t seed, cu
     const double root = std::sqrt(2.0 * n);
     double ratio_sum = 0.0;
     for (int k = 0; k < pairs; ++k) {
-        random_rhs(m.b, m.ndof, rng, st);
+        if (lrn.use_recorded)   // a coarse right-hand side of the run's own V-cycles
+            blas::copy(lrn.rec.as<float2>() + (size_t)k * m.ndof, m.b.ptr, m.ndof, TDZ_FP32, st);
+        else
+            random_rhs(m.b, m.ndof, rng, st);
         chebyshev(m, TDZ_FP32, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);   // production solve
         blas::copy(m.x.ptr, x0.ptr, m.ndof, TDZ_FP32, st);
         m.opp->apply(TDZ_STAGE, TDZ_FP32, x0.ptr, m.t1.ptr, st);

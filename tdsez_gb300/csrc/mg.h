@@ -68,6 +68,11 @@ struct LearnedCoarse {
     DevBuf in, out, scale;       // planar [2][n] FP32 (batch 1), device ||r||
     DevBuf pin, ptgt;            // training pairs [pairs][2][n]
     int npairs = 0;
+    // coarsest-level right-hand sides recorded from the V-cycles of a run
+    // (the propagator's own stage solves), the inputs of the training pairs
+    DevBuf rec;
+    int rec_cap = 0, rec_n = 0;
+    bool use_recorded = false;   // train_coarse takes its inputs from rec
     float cscale = 1.f;          // mean ||e|| / ||r|| of the training pairs (output scale)
 };
 
@@ -90,6 +95,11 @@ struct Multigrid : Precond {
     // generate `pairs` pairs at the coarsest level for the current stage and
     // train for `epochs` passes; returns the mean relative loss of the last epoch
     float train_coarse(int pairs, int epochs, float lr, uint64_t seed, cudaStream_t st);
+    // record the coarsest right-hand side of the next `capacity` V-cycles
+    // (0: stop recording, keep what was recorded)
+    void record_coarse(int capacity);
+    // train on the recorded right-hand sides (all of them) instead of random ones
+    float train_recorded(int epochs, float lr, uint64_t seed, cudaStream_t st);
     // relative error ||e - c|| / ||e|| of the corrected coarse solve c against
     // e = A_c^-1 b on `trials` fresh random right-hand sides, without (first)
     // and with (second) the network

@@ -338,6 +338,10 @@ void Multigrid::vcycle(int l, cudaStream_t st) {
     MGLevel &m = lv[l];
     const int last = (int)lv.size() - 1;
     if (l == last) {
+        if (lrn.on && lrn.rec_n < lrn.rec_cap) {   // a training input from this run
+            blas::copy(m.b.ptr, lrn.rec.as<float2>() + (size_t)lrn.rec_n * m.ndof, m.ndof, TDZ_FP32, st);
+            ++lrn.rec_n;
+        }
         chebyshev(m, prec, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);
         if (lrn.on && lrn.trained) coarse_correct(m, st);
         return;

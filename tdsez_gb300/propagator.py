@@ -194,6 +194,19 @@ class Propagator:
         return {"solves": s.value, "its": i.value, "applies": a.value, "cycles": cy.value,
                 "last_its": li.value, "last_rres": rr.value}
 
+    def record_coarse(self, capacity: int):
+        """Record the coarsest right-hand sides of the next ``capacity``
+        V-cycles of each stage solver (pc="mg", mg_learned=True); 0 stops."""
+        _lib.check(_lib.load().tdz_prop_record_coarse(self.handle, capacity))
+
+    def train_coarse(self, epochs: int = 30, lr: float = 1e-3, seed: int = 20261203, stream=None):
+        """Train the learned coarse correction on the recorded right-hand
+        sides; returns (last-epoch loss, pairs)."""
+        loss, pairs = C.c_float(), C.c_int()
+        _lib.check(_lib.load().tdz_prop_train_coarse(self.handle, epochs, lr, seed, C.byref(loss), C.byref(pairs),
+                                                     C.c_void_p(_stream(stream))))
+        return loss.value, pairs.value
+
     def refreshes(self) -> int:
         """Preconditioner rebuilds the refresh rule asked for so far."""
         n = C.c_longlong()
