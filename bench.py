@@ -412,27 +412,26 @@ def learned_arms(args, op, psi0, w, stream):
               mg_coarse_its=args.mg_coarse_its, mg_levels=args.learned_levels)
     out = {}
     G = Propagator(op, "cn", field=w.field, mg_learned=True, **kw)
-    psi = psi0.clone()
+    G0 = Propagator(op, "cn", field=w.field, **kw)
+    psi, psi_p = psi0.clone(), psi0.clone()
     t = 0.0
     G.record_coarse(args.learned_pairs)
     t0 = time.time()
-    for _ in range(args.learned_train_steps):
+    for _ in range(args.learned_train_steps):   # both arms take these steps (same guess history)
         G.step(psi, t, dt)
+        G0.step(psi_p, t, dt)
         t += dt
     G.record_coarse(0)
     loss, pairs = G.train_coarse(epochs=args.learned_epochs, lr=1e-3)
     torch.cuda.synchronize()
     train_s = time.time() - t0
     t_start = t
-    psi_start = psi.clone()
     sps, its, _ = _timed_steps(G, psi, t_start, dt, args.warmup, args.learned_steps, stream)
     out["learned"] = {"steps_per_s": sps, "its_per_step": its, "levels": args.learned_levels,
                       "train_pairs": pairs, "train_loss": loss, "train_steps": args.learned_train_steps,
                       "train_epochs": args.learned_epochs, "train_s": train_s, "steps": args.learned_steps,
                       "what": "FP32 multigrid with the CNN coarse correction (BF16 weights) in FP64 FGMRES"}
-    G0 = Propagator(op, "cn", field=w.field, **kw)
-    psi = psi_start.clone()
-    sps0, its0, _ = _timed_steps(G0, psi, t_start, dt, args.warmup, args.learned_steps, stream)
+    sps0, its0, _ = _timed_steps(G0, psi_p, t_start, dt, args.warmup, args.learned_steps, stream)
     out["plain"] = {"steps_per_s": sps0, "its_per_step": its0, "levels": args.learned_levels,
                     "steps": args.learned_steps, "what": "the same hierarchy without the network"}
     return out

@@ -70,29 +70,29 @@ def test_learned_correction_trained_on_the_propagation(cuda):
     S = Space(w.knots, w.p, w.nq)
     op = Operator(S, w.phys)
     kw = dict(pc="mg", precision="fp32", outer="df", rtol=1e-10, mg_levels=2)
-    G = Propagator(op, "cn", field=w.field, mg_learned=True, **kw)
-    psi = op.separable_state(w.packet)
+    props = {"learned": Propagator(op, "cn", field=w.field, mg_learned=True, **kw),
+             "plain": Propagator(op, "cn", field=w.field, **kw),
+             "fdm": Propagator(op, "cn", field=w.field, pc="fdm", precision="fp32", outer="df", rtol=1e-10)}
+    psi0 = op.separable_state(w.packet)
     t, dt = 0.0, w.dt
-    G.record_coarse(64)
-    for _ in range(6):
-        G.step(psi, t, dt)
+    x = {k: psi0.clone() for k in props}
+    props["learned"].record_coarse(64)
+    for _ in range(6):   # the same first steps for every arm (and the same guess history)
+        for k, P in props.items():
+            P.step(x[k], t, dt)
         t += dt
-    G.record_coarse(0)
-    loss, pairs = G.train_coarse(epochs=40, lr=1e-3)
+    props["learned"].record_coarse(0)
+    loss, pairs = props["learned"].train_coarse(epochs=40, lr=1e-3)
     assert pairs >= 8 and np.isfinite(loss) and loss < 1.0, (loss, pairs)
-    start = psi.clone()
     states, its = {}, {}
-    for name, P in (("learned", G), ("plain", Propagator(op, "cn", field=w.field, **kw)),
-                    ("fdm", Propagator(op, "cn", field=w.field, pc="fdm", precision="fp32", outer="df", rtol=1e-10,
-                                       guess_order=-1))):
-        x = start.clone()
+    for name, P in props.items():
         s0 = P.stats()
         for k in range(4):
-            P.step(x, t + k * dt, dt)
+            P.step(x[name], t + k * dt, dt)
         torch.cuda.synchronize()
         s1 = P.stats()
         its[name] = (s1["its"] - s0["its"]) / 4
-        states[name] = x
+        states[name] = x[name]
     print(f"training pairs {pairs}, loss {loss:.3e}; FGMRES its/step: learned {its['learned']}, "
           f"plain {its['plain']}, FDM {its['fdm']}")
     for name in ("learned", "plain"):
