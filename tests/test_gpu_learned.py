@@ -95,7 +95,11 @@ def test_learned_correction_trained_on_the_propagation(cuda):
         states[name] = x[name]
     print(f"training pairs {pairs}, loss {loss:.3e}; FGMRES its/step: learned {its['learned']}, "
           f"plain {its['plain']}, FDM {its['fdm']}")
+    # each stage solve stops at a relative residual of 1e-10; with the stage
+    # operator's conditioning (its spectrum spans |1 + i dt/2 lambda| up to a
+    # few hundred) the states of independent solvers differ by up to ~1e-8 per
+    # step, accumulated over ten steps
     for name in ("learned", "plain"):
         rel = (torch.linalg.norm(states[name] - states["fdm"]) / torch.linalg.norm(states["fdm"])).item()
-        assert rel < 1e-8, (name, rel)
+        assert rel < 1e-6, (name, rel)
     assert its["learned"] <= its["plain"], its
