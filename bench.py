@@ -370,14 +370,15 @@ def run_tdz(args):
         # vectors, 32 algorithmic bytes per coefficient (x read, y written once). It is bound by the
         # FP32 pipes (double-float arithmetic), so its HBM fraction is low by construction; traffic is
         # dram read + write of one launch from the ncu capture in profiles/.
-        "roofline": {"kernel": "k_apply3d<dff> double-float stage apply (FGMRES residual and Arnoldi)",
+        "roofline": {"kernel": "k_apply3d_rb<dff> double-float stage apply (FGMRES residual)",
                      "bound": "hbm", "achieved": bytes64 / tdf / 1e9, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                      "frac": bytes64 / tdf / 1e9 / pk.get("hbm_gbs", 6800.0), "traffic": DF_APPLY_TRAFFIC,
                      "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
                      "launch_us": tdf * 1e6, "bytes_per_launch": bytes64,
-                     "limiter": "FP32 pipes: 12 FP32 instructions per double-float FMA (ncu: 64.8% issue, "
-                                "52.1% FMA pipe)",
-                     "fp32_apply": {"kernel": "k_apply3d<float> (multigrid smoother and residual)",
+                     "limiter": "FP32 pipes: 12 FP32 instructions per double-float FMA (ncu: 70% issue, "
+                                "55% FMA pipe)",
+                     "fp32_apply": {"kernel": "k_apply3d_rb<float> (multigrid smoother and residual; latency-bound, "
+                                              "ncu: 57% issue, 24% warps active)",
                                     "achieved": ach32, "frac": ach32 / pk.get("hbm_gbs", 6800.0),
                                     "launch_us": t32 * 1e6, "bytes_per_launch": bytes32},
                      "fp64_apply": {"kernel": "k_apply3d<double> (native FP64, not used by the step)",
@@ -396,11 +397,11 @@ def run_tdz(args):
 
 CPU_GRID = (16, 16, 32)
 CPU_GRID2 = (20, 20, 40)
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_apply3d<dff,3,0,1> launch on the
-# 160x160x320 workload at its tuned launch shape (16 x 16 tiles, 303 CTAs; ncu --set full,
-# profiles/k_apply3d_df_stage_heterostructure_160x160x320_p3.md). The narrow tiles re-read
-# their x / y halos, which the FP32-pipe-bound kernel can afford.
-DF_APPLY_TRAFFIC = 297.75e6 + 125.24e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_apply3d_rb<dff> CN stage apply on
+# the 160x160x320 workload (ncu --set full, tile 32 x run 73;
+# profiles/k_apply3d_rb_df_stage_heterostructure_160x160x320_p3.md). Writes still in L2
+# when the launch ends are not counted; the halo re-reads of neighbouring tiles are.
+DF_APPLY_TRAFFIC = 206.87e6 + 109.77e6
 
 
 def learned_arms(args, op, psi0, w, stream):
