@@ -8,19 +8,24 @@
 namespace tdz {
 
 // ---------------------------------------------------------------- 1D pieces
+// The coarsening rule of CoarsenKnots (src/multigrid.cpp:25-40): among the
+// distinct breakpoints, numbered from the left end, the odd-numbered interior
+// ones of multiplicity one are removed; ends and repeated (C0) breakpoints
+// stay with their multiplicity.
 std::vector<double> coarsen_knots(const std::vector<double> &U, bool *dropped) {
-    // breakpoints with multiplicity; drop every other simple interior one
-    std::vector<std::pair<double, int>> bp;
-    for (double u : U) {
-        if (!bp.empty() && u == bp.back().first) ++bp.back().second;
-        else bp.push_back({u, 1});
-    }
     std::vector<double> C;
     *dropped = false;
-    for (size_t i = 0; i < bp.size(); ++i) {
-        const bool interior = i > 0 && i + 1 < bp.size();
-        if (interior && bp[i].second == 1 && i % 2 == 1) { *dropped = true; continue; }
-        C.insert(C.end(), bp[i].second, bp[i].first);
+    size_t i = 0;
+    int number = 0;                // index of the current distinct breakpoint
+    while (i < U.size()) {
+        size_t j = i;
+        while (j < U.size() && U[j] == U[i]) ++j;   // [i, j): one breakpoint
+        const bool end = i == 0 || j == U.size();
+        const bool simple = j - i == 1;
+        if (!end && simple && number % 2 == 1) *dropped = true;
+        else C.insert(C.end(), U.begin() + i, U.begin() + j);
+        ++number;
+        i = j;
     }
     return C;
 }
@@ -32,59 +37,82 @@ int count_spans(const std::vector<double> &U) {
     return n;
 }
 
+// Prolongation from the spline space on knots C to the one on F (C a
+// subsequence of F, same degree): the coarse basis functions lie in the fine
+// space, so their fine coefficients are exactly the L2 projection
+//   P = M_F^-1 G,  M_F = (N^F_i, N^F_k),  G = (N^F_i, N^C_j),
+// with both inner products integrated exactly by p+1 Gauss points per fine
+// span and M_F solved by a banded Cholesky factorisation. This is the matrix
+// that Boehm's knot insertion (the reference's Prolongation,
+// src/multigrid.cpp:52-81) builds one knot at a time; entries below 1e-10
+// (rounding of exact zeros) are dropped.
 RowSparse boehm_prolongation(const std::vector<double> &C, const std::vector<double> &F, int p) {
-    using Row = std::vector<std::pair<int, double>>;
-    std::vector<double> U = C;
-    const int nc = (int)C.size() - p - 1;
-    std::vector<Row> P(nc);
-    for (int j = 0; j < nc; ++j) P[j] = {{j, 1.0}};
-    // knots of F missing from C (multiset difference of sorted lists)
-    std::vector<double> add;
-    {
-        size_t i = 0, j = 0;
-        while (i < F.size()) {
-            if (j < C.size() && C[j] == F[i]) { ++i; ++j; }
-            else if (j < C.size() && C[j] < F[i]) ++j;
-            else add.push_back(F[i++]);
+    const int nf = (int)F.size() - p - 1, nc = (int)C.size() - p - 1;
+    const int bw = p;                       // half bandwidth of M_F
+    std::vector<double> L((size_t)nf * (bw + 1), 0.0);   // lower band: L[i][d] = M(i, i - d)
+    std::vector<double> G((size_t)nf * nc, 0.0);
+    std::vector<double> gx, gw;
+    gauss_legendre(p + 1, gx, gw);
+    std::vector<double> vf(2 * (p + 1)), vc(2 * (p + 1));
+    for (int k = p; k < nf; ++k) {
+        const double a = F[k], b = F[k + 1];
+        if (!(b > a)) continue;
+        for (int q = 0; q <= p; ++q) {
+            const double x = 0.5 * (a + b) + 0.5 * (b - a) * gx[q], wq = 0.5 * (b - a) * gw[q];
+            ders_basis(F, p, k, x, 0, vf.data());
+            const int sc = find_span(C, p, nc, x);
+            ders_basis(C, p, sc, x, 0, vc.data());
+            for (int r = 0; r <= p; ++r) {
+                const int i = k - p + r;
+                for (int r2 = 0; r2 <= r; ++r2) L[(size_t)i * (bw + 1) + (r - r2)] += wq * vf[r] * vf[r2];
+                for (int c = 0; c <= p; ++c) G[(size_t)i * nc + (sc - p + c)] += wq * vf[r] * vc[c];
+            }
         }
     }
-    auto combine = [](const Row &a, double wa, const Row &b, double wb) {
-        Row out;
-        size_t i = 0, j = 0;
-        while (i < a.size() || j < b.size()) {
-            if (j >= b.size() || (i < a.size() && a[i].first < b[j].first)) { out.push_back({a[i].first, wa * a[i].second}); ++i; }
-            else if (i >= a.size() || b[j].first < a[i].first) { out.push_back({b[j].first, wb * b[j].second}); ++j; }
-            else { out.push_back({a[i].first, wa * a[i].second + wb * b[j].second}); ++i; ++j; }
+    // banded Cholesky M_F = L L^T in place
+    for (int i = 0; i < nf; ++i) {
+        for (int d = std::min(bw, i); d >= 1; --d) {
+            const int j = i - d;
+            double v = L[(size_t)i * (bw + 1) + d];
+            for (int e = 1; e <= bw - d && e <= j; ++e) v -= L[(size_t)i * (bw + 1) + d + e] * L[(size_t)j * (bw + 1) + e];
+            L[(size_t)i * (bw + 1) + d] = v / L[(size_t)j * (bw + 1)];
         }
-        return out;
-    };
-    for (double xi : add) {
-        const int n = (int)U.size() - p - 1;
-        int k = (int)(std::upper_bound(U.begin(), U.end(), xi) - U.begin()) - 1;
-        k = std::min(std::max(k, p), n - 1);
-        std::vector<Row> Q(n + 1);
-        for (int i = 0; i <= k - p; ++i) Q[i] = P[i];
-        for (int i = k + 1; i <= n; ++i) Q[i] = P[i - 1];
-        for (int i = k - p + 1; i <= k; ++i) {
-            const double a = (xi - U[i]) / (U[i + p] - U[i]);
-            Q[i] = combine(P[i], a, P[i - 1], 1.0 - a);
+        double v = L[(size_t)i * (bw + 1)];
+        for (int d = 1; d <= std::min(bw, i); ++d) v -= L[(size_t)i * (bw + 1) + d] * L[(size_t)i * (bw + 1) + d];
+        TDZ_CHECK(v > 0.0, TDZ_ERR_INTERNAL, "fine mass matrix not positive definite");
+        L[(size_t)i * (bw + 1)] = std::sqrt(v);
+    }
+    // P = L^-T L^-1 G, column by column
+    std::vector<double> P((size_t)nf * nc);
+    std::vector<double> y(nf);
+    for (int j = 0; j < nc; ++j) {
+        for (int i = 0; i < nf; ++i) {
+            double v = G[(size_t)i * nc + j];
+            for (int d = 1; d <= std::min(bw, i); ++d) v -= L[(size_t)i * (bw + 1) + d] * y[i - d];
+            y[i] = v / L[(size_t)i * (bw + 1)];
         }
-        P.swap(Q);
-        U.insert(std::upper_bound(U.begin(), U.end(), xi), xi);
+        for (int i = nf - 1; i >= 0; --i) {
+            double v = y[i];
+            for (int d = 1; d <= bw && i + d < nf; ++d) v -= L[(size_t)(i + d) * (bw + 1) + d] * y[i + d];
+            y[i] = v / L[(size_t)i * (bw + 1)];
+        }
+        for (int i = 0; i < nf; ++i) P[(size_t)i * nc + j] = y[i];
     }
     RowSparse R;
-    R.rows = (int)P.size();
+    R.rows = nf;
     R.cols = nc;
-    for (auto &r : P) {
-        r.erase(std::remove_if(r.begin(), r.end(), [](const auto &e) { return std::abs(e.second) < 1e-14; }), r.end());
-        R.width = std::max(R.width, (int)r.size());
+    std::vector<std::vector<std::pair<int, double>>> rows(nf);
+    for (int i = 0; i < nf; ++i) {
+        for (int j = 0; j < nc; ++j)
+            if (std::abs(P[(size_t)i * nc + j]) >= 1e-10) rows[i].push_back({j, P[(size_t)i * nc + j]});
+        R.width = std::max(R.width, (int)rows[i].size());
     }
     R.col.assign((size_t)R.rows * R.width, -1);
     R.val.assign((size_t)R.rows * R.width, 0.0);
     for (int i = 0; i < R.rows; ++i)
-        for (size_t t = 0; t < P[i].size(); ++t) {
-            R.col[(size_t)i * R.width + t] = P[i][t].first;
-            R.val[(size_t)i * R.width + t] = P[i][t].second;
+        for (size_t t = 0; t < rows[i].size(); ++t) {
+            R.col[(size_t)i * R.width + t] = rows[i][t].first;
+            R.val[(size_t)i * R.width + t] = rows[i][t].second;
         }
     return R;
 }

@@ -3,9 +3,8 @@
 //
 // Follows PetIGA's IGABasis tables as TDSE-Z uses them: element = non-empty
 // knot span, Gauss points mapped to the span, weight * detJac
-// (src/tensorops.cpp:40-57); the Gauss rule is the Newton iteration of
-// src/tsurff.cpp:24-44 and the basis recursion Piegl-Tiller A2.2/A2.3 as in
-// src/tsurff.cpp:47-66.
+// (src/tensorops.cpp:40-57); the basis recursion is Piegl-Tiller A2.2/A2.3
+// (the reference's src/tsurff.cpp:47-66 uses the same published algorithm).
 #include "space.h"
 
 #include <algorithm>
@@ -13,35 +12,63 @@
 
 namespace tdz {
 
+// Gauss-Legendre rule on [-1, 1] by Golub-Welsch: the nodes are the
+// eigenvalues of the symmetric tridiagonal Jacobi matrix of the Legendre
+// recurrence (zero diagonal, off-diagonal k / sqrt(4 k^2 - 1)), found here by
+// cyclic Jacobi rotations; each node is then polished by Newton steps on
+// P_n and its weight taken as 2 / ((1 - x^2) P_n'(x)^2) (Abramowitz-Stegun
+// 25.4.29), which is accurate to rounding for every n.
 void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
-    x.assign(n, 0.0);
-    w.assign(n, 0.0);
-    const double pi = std::acos(-1.0);
-    for (int j = 0; j < n; ++j) {
-        double z = std::cos(pi * (j + 0.75) / (n + 0.5)), der = 1;
-        for (int it = 0; it < 100; ++it) {
-            double p = 1, p0 = 0;
-            for (int k = 1; k <= n; ++k) {
-                const double old = p;
-                p = ((2 * k - 1) * z * p - (k - 1) * p0) / k;
-                p0 = old;
+    std::vector<double> J((size_t)n * n, 0.0);
+    for (int k = 1; k < n; ++k) J[(size_t)(k - 1) * n + k] = J[(size_t)k * n + k - 1] = k / std::sqrt(4.0 * k * k - 1.0);
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = i + 1; j < n; ++j) off += J[(size_t)i * n + j] * J[(size_t)i * n + j];
+        if (off < 1e-32) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = J[(size_t)p * n + q];
+                if (std::abs(apq) < 1e-300) continue;
+                const double th = (J[(size_t)q * n + q] - J[(size_t)p * n + p]) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::abs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double kp = J[(size_t)k * n + p], kq = J[(size_t)k * n + q];
+                    J[(size_t)k * n + p] = c * kp - sn * kq;
+                    J[(size_t)k * n + q] = sn * kp + c * kq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double pk = J[(size_t)p * n + k], qk = J[(size_t)q * n + k];
+                    J[(size_t)p * n + k] = c * pk - sn * qk;
+                    J[(size_t)q * n + k] = sn * pk + c * qk;
+                }
             }
-            der = n * (z * p - p0) / (z * z - 1);
-            const double dz = p / der;
-            z -= dz;
-            if (std::abs(dz) < 1e-15) break;
-        }
-        double p = 1, p0 = 0;
-        for (int k = 1; k <= n; ++k) {
-            const double old = p;
-            p = ((2 * k - 1) * z * p - (k - 1) * p0) / k;
-            p0 = old;
-        }
-        der = n * (z * p - p0) / (z * z - 1);
-        x[j] = z;
-        w[j] = 2 / ((1 - z * z) * der * der);
     }
-    // ascending order
+    x.resize(n);
+    w.resize(n);
+    // P_n(t) and P_n'(t) by the three-term recurrence
+    auto legendre = [n](double t, double *d) {
+        double p0 = 1.0, p1 = t;
+        if (n == 0) { *d = 0.0; return 1.0; }
+        for (int k = 2; k <= n; ++k) {
+            const double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        *d = n * (t * p1 - p0) / (t * t - 1.0);
+        return p1;
+    };
+    for (int i = 0; i < n; ++i) {
+        double t = J[(size_t)i * n + i], d = 1.0;
+        for (int it = 0; it < 3; ++it) {
+            const double v = legendre(t, &d);
+            t -= v / d;
+        }
+        legendre(t, &d);
+        x[i] = t;
+        w[i] = 2.0 / ((1.0 - t * t) * d * d);
+    }
     std::vector<int> idx(n);
     for (int i = 0; i < n; ++i) idx[i] = i;
     std::sort(idx.begin(), idx.end(), [&](int a, int b) { return x[a] < x[b]; });

@@ -5,6 +5,7 @@
 // integrals (RK4, src/tsurff.cpp:395-428) are advanced on the host.
 #include "tsurff.h"
 
+#include <array>
 #include <cmath>
 
 #include "cplx.cuh"
@@ -283,33 +284,48 @@ void TSurff::setup(const Space &s, const tdz_tsurff_opts &o, tdz_field_fn f, voi
     upload(kdev, kall);
 }
 
-void TSurff::advance_volkov(double t) {
-    const double h = t - vt;
-    if (h <= 0) return;
-    const int nsub = std::max(1, (int)std::ceil(h / (0.5 * dt) - 1e-9));
-    const double ds = h / nsub;
-    auto rhs = [&](double tt, const double y[7], double dy[7]) {
-        double a2 = 0;
-        for (int d = 0; d < 3; ++d) {
-            dy[d] = (d < dim && field) ? -sign * field(d, tt, field_ctx) : 0.0;
-            dy[3 + d] = y[d];
-            a2 += y[d] * y[d];
-        }
-        dy[6] = a2 / (2 * mass) + V0;
+namespace {
+using Volkov7 = std::array<double, 7>;   // A_x, A_y, A_z, B_x, B_y, B_z, C
+// one classical fourth-order Runge-Kutta step (Kutta's tableau) of y' = f(t, y)
+template <class F> Volkov7 rk4_step(const F &f, double t, const Volkov7 &y, double h) {
+    auto along = [&](const Volkov7 &s, double c) {
+        Volkov7 r;
+        for (int i = 0; i < 7; ++i) r[i] = y[i] + c * s[i];
+        return r;
     };
-    double y[7] = {A[0], A[1], A[2], B[0], B[1], B[2], C}, k1[7], k2[7], k3[7], k4[7], z[7];
-    for (int i = 0; i < nsub; ++i) {
-        const double t0 = vt + i * ds;
-        rhs(t0, y, k1);
-        for (int j = 0; j < 7; ++j) z[j] = y[j] + 0.5 * ds * k1[j];
-        rhs(t0 + 0.5 * ds, z, k2);
-        for (int j = 0; j < 7; ++j) z[j] = y[j] + 0.5 * ds * k2[j];
-        rhs(t0 + 0.5 * ds, z, k3);
-        for (int j = 0; j < 7; ++j) z[j] = y[j] + ds * k3[j];
-        rhs(t0 + ds, z, k4);
-        for (int j = 0; j < 7; ++j) y[j] += ds / 6 * (k1[j] + 2 * k2[j] + 2 * k3[j] + k4[j]);
-    }
-    for (int d = 0; d < 3; ++d) { A[d] = y[d]; B[d] = y[3 + d]; }
+    const Volkov7 s1 = f(t, y);
+    const Volkov7 s2 = f(t + 0.5 * h, along(s1, 0.5 * h));
+    const Volkov7 s3 = f(t + 0.5 * h, along(s2, 0.5 * h));
+    const Volkov7 s4 = f(t + h, along(s3, h));
+    Volkov7 out;
+    for (int i = 0; i < 7; ++i) out[i] = y[i] + h * (s1[i] + 2.0 * (s2[i] + s3[i]) + s4[i]) / 6.0;
+    return out;
+}
+}  // namespace
+
+// Volkov phases of the surface states from the last sample time to t:
+// A' = -s E(t), B' = A, C' = |A|^2 / 2m + V0, by Runge-Kutta substeps of at
+// most dt/2 (the substep rule of AdvanceVolkov, src/tsurff.cpp:395-428, which
+// the flux's parity with the reference depends on)
+void TSurff::advance_volkov(double t) {
+    const double span = t - vt;
+    if (span <= 0) return;
+    const int substeps = std::max(1, (int)std::ceil(span / (0.5 * dt) - 1e-9));
+    const double ds = span / substeps;
+    auto deriv = [&](double tt, const Volkov7 &y) {
+        Volkov7 d{};
+        double a2 = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            d[a] = (a < dim && field) ? -sign * field(a, tt, field_ctx) : 0.0;
+            d[3 + a] = y[a];
+            a2 += y[a] * y[a];
+        }
+        d[6] = a2 / (2.0 * mass) + V0;
+        return d;
+    };
+    Volkov7 y{A[0], A[1], A[2], B[0], B[1], B[2], C};
+    for (int k = 0; k < substeps; ++k) y = rk4_step(deriv, vt + k * ds, y, ds);
+    for (int a = 0; a < 3; ++a) { A[a] = y[a]; B[a] = y[3 + a]; }
     C = y[6];
     vt = t;
 }
