@@ -183,6 +183,10 @@ typedef struct tdz_solver tdz_solver;
 #define TDZ_PC_FDM 3  /* fast diagonalisation: exact FP32 inverse of operators
                          whose inner axes carry only mass and stiffness (the
                          z-layered structure), approximate otherwise          */
+#define TDZ_PC_BAND 4 /* 1D: exact banded LU with partial pivoting (FP64) of
+                         the stage operator, refactored when the refresh rule
+                         asks (tdz_pc_refresh_stale) or the end term moves to
+                         its next energy                                      */
 typedef struct tdz_solver_opts {
     int restart;        /* Krylov restart; 0 = 30, or 50 above 100000 rows   */
     int maxit;          /* iteration cap; 0 = 1000                           */
@@ -431,6 +435,35 @@ tdz_status tdz_tsurff_amplitudes(tdz_tsurff *ts, double *out, void *stream);
  * all of the wave packet has left the box. out (host): prod(nk) complex
  * values, k_x slowest. Synchronises the stream. */
 tdz_status tdz_tsurff_interior(tdz_tsurff *ts, const void *psi, double *out, void *stream);
+/* End term: the flux still to cross the surface after the last sample time
+ * T, for a run that ends after the pulse (TDSEZTSurff::EndTerm,
+ * src/tsurff.cpp:650-976; SurffEndTerm = 1). With the field off after T,
+ *   b_end(k) = flux_k(T)[phi_E],  (E M - H) phi_E = i M psi(T),  E = |k + A(T)|^2/2m + V0,
+ * H the field-free Hamiltonian of op including its absorbing layer (required:
+ * it is the outgoing-wave condition). phi_E is solved on energy nodes uniform
+ * in p = |k + A(T)| (spacing dp; automatic: min(grid spacing, 0.25/(R sqrt d)),
+ * refined to 0.25/(L sqrt d) below 2 k_cap, k_cap = 6.555 / cap_width, L the
+ * largest box half-width) and the node fluxes are combined with four-point
+ * Lagrange weights in p. Every node is one FGMRES solve (FP64, relative
+ * residual rtol) on the device, warm-started from the previous node, with
+ * the preconditioner of `inner` (NULL: the exact banded LU in 1D, the FDM
+ * inverse in 2D/3D, built for the damped pole E (1 + i eta) when it is not
+ * exact). psi: psi(T) (FP64 device vector), sampled at T before the call.
+ * out (host): prod(nk) complex values, k_x slowest, to be added to
+ * tdz_tsurff_amplitudes. stats (host, may be NULL, 6 doubles): nodes, total
+ * FGMRES iterations, largest per node, largest node spacing, eta used,
+ * seconds. Fails (TDZ_ERR_ARG) when the field is not over at T. The
+ * operator's stage coefficients are overwritten. */
+typedef struct tdz_tsurff_end_opts {
+    double dp;          /* node spacing in p (SurffEndTermDk); 0 = automatic  */
+    double cap_width;   /* absorbing-layer width; needed when dp = 0          */
+    double eta;         /* preconditioner pole damping; < 0 = automatic      */
+    double rtol;        /* per-node relative residual; 0 = 1e-10              */
+    int maxit;          /* per-node FGMRES iterations; 0 = 4000               */
+} tdz_tsurff_end_opts;
+tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts *inner,
+                               const tdz_tsurff_end_opts *o, const void *psi, double *out, double *stats,
+                               void *stream);
 /* Volkov integrals at the last sample: A[3], B[3], C, t (8 doubles). */
 tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct);
 void tdz_tsurff_destroy(tdz_tsurff *ts);

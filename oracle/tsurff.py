@@ -8,13 +8,16 @@
   substeps of at most TimeStep/2 (``tsurff.cpp:395-428``);
 * flux per momentum (``FluxList``, ``tsurff.cpp:536-559``; the grid path
   ``FluxGrid`` ``:478-534`` is the same sum factorised by axis);
-* trapezoid accumulation over samples (``AddFlux``, ``tsurff.cpp:439-469``).
+* trapezoid accumulation over samples (``AddFlux``, ``tsurff.cpp:439-469``);
+* the end term (``EndTerm``, ``tsurff.cpp:650-976``) with one direct sparse
+  solve per energy node in place of the reference's multi-shift Arnoldi.
 """
 from __future__ import annotations
 
 import math
 
 import numpy as np
+import scipy.sparse.linalg as sla
 
 from .bspline import Space, find_span, ders_basis, gauss_legendre
 
@@ -191,3 +194,78 @@ class OracleTSurff:
             phi = phi + self.vt * kd * kd / (2 * self.mass) + kd * self.B[d] / self.mass
         out = (2 * math.pi) ** (-0.5 * self.dim) * np.exp(1j * phi) * G
         return np.moveaxis(out, list(range(self.dim)), list(reversed(range(self.dim)))).reshape(-1)
+
+
+# --------------------------------------------------------------------------
+# End term (SurffEndTerm = 1, ``src/tsurff.cpp:650-976``)
+# --------------------------------------------------------------------------
+
+def end_nodes(pmin, pmax, split, dp_in, dp_out):
+    """Energy nodes in p = |k + A(T)| (``tsurff.cpp:700-723``): spacing dp_in
+    on [pmin, split], dp_out on [split, pmax], midpoints added until there
+    are four."""
+    if not pmax > pmin:
+        return np.array([pmin])
+    node = []
+
+    def segment(a, b, dp):
+        if not b > a:
+            return
+        cnt = max(1, int(math.ceil((b - a) / dp - 1e-9)))
+        for i in range(0 if not node else 1, cnt + 1):
+            node.append(a + (b - a) * i / cnt)
+    segment(pmin, split, dp_in)
+    segment(node[-1] if node else pmin, pmax, dp_out)
+    while len(node) < 4:
+        finer = []
+        for a, b in zip(node[:-1], node[1:]):
+            finer += [a, 0.5 * (a + b)]
+        node = finer + [node[-1]]
+    return np.array(node)
+
+
+def lagrange_weights(node, p):
+    """(first node, weights) of the four-point Lagrange interpolation in p
+    around p (``tsurff.cpp:725-756``)."""
+    nn = len(node)
+    if nn == 1:
+        return 0, np.array([1.0])
+    m = min(nn, 4)
+    below = int(np.searchsorted(node, p, side="right")) - 1
+    j0 = max(0, min(nn - m, below - 1))
+    w = np.ones(m)
+    for a in range(m):
+        for b in range(m):
+            if b != a:
+                w[a] *= (p - node[j0 + b]) / (node[j0 + a] - node[j0 + b])
+    return j0, w
+
+
+def end_term(ts: OracleTSurff, psi, M, H, kgrid, cap_width=0.0, dp=0.0):
+    """End-term amplitudes of ``ts`` after its last sample (time T, Volkov
+    state at T): per energy node E_j = p_j^2/2m + V0 the direct sparse solve
+    of (E_j M - H) phi_j = i M psi(T) (H with the CAP), the flux of phi_j at
+    T on every momentum, combined with the Lagrange weights of each momentum.
+    Returns (amplitudes, nodes)."""
+    ks = [np.asarray(kgrid[d]) if d < ts.dim else np.array([0.0]) for d in range(3)]
+    K = np.stack(np.meshgrid(*ks, indexing="ij"), axis=-1).reshape(-1, 3)
+    pk = np.linalg.norm(K + ts.A[None, :], axis=1)
+    dk = min([(k[-1] - k[0]) / (len(k) - 1) for k in ks[:ts.dim] if len(k) > 1] or [np.inf])
+    L = max(max(abs(a.knots[0]), abs(a.knots[-1])) for a in ts.space.axes)
+    sd = math.sqrt(ts.dim)
+    kcap = 6.555 / cap_width if cap_width > 0 else 0.0
+    dp_out = dp if dp > 0 else min(dk, 0.25 / (ts.R * sd))
+    dp_in = dp if dp > 0 else min(dp_out, 0.25 / (L * sd))
+    split = min(max(2 * kcap, pk.min()), pk.max())
+    node = end_nodes(pk.min(), pk.max(), split, dp_in, dp_out)
+    W = np.zeros((len(node), len(K)))
+    for q, p in enumerate(pk):
+        j0, w = lagrange_weights(node, p)
+        W[j0:j0 + len(w), q] = w
+    b = 1j * (M @ psi)
+    amp = np.zeros(len(K), dtype=np.complex128)
+    for j, p in enumerate(node):
+        E = p * p / (2 * ts.mass) + ts.V0
+        phi = sla.splu((E * M - H).astype(np.complex128).tocsc()).solve(b)
+        amp += W[j] * ts.flux(phi, kgrid)
+    return amp, node

@@ -76,9 +76,19 @@ class tdz_tsurff_opts(C.Structure):
     ]
 
 
+class tdz_tsurff_end_opts(C.Structure):
+    _fields_ = [
+        ("dp", C.c_double),
+        ("cap_width", C.c_double),
+        ("eta", C.c_double),
+        ("rtol", C.c_double),
+        ("maxit", C.c_int),
+    ]
+
+
 FIELD_FN = C.CFUNCTYPE(C.c_double, C.c_int, C.c_double, C.c_void_p)
 
-TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG, TDZ_PC_FDM = 0, 1, 2, 3
+TDZ_PC_NONE, TDZ_PC_MASS, TDZ_PC_MG, TDZ_PC_FDM, TDZ_PC_BAND = 0, 1, 2, 3, 4
 TDZ_CN, TDZ_PADE22, TDZ_MAGNUS4 = 0, 1, 2
 
 _lib = None
@@ -123,6 +133,7 @@ SIGNATURES = {
     "tdz_tsurff_amplitudes": (I, [VP, C.POINTER(D), VP]),
     "tdz_tsurff_volkov": (I, [VP, C.POINTER(D)]),
     "tdz_tsurff_interior": (I, [VP, VP, C.POINTER(D), VP]),
+    "tdz_tsurff_end_term": (I, [VP, VP, C.c_void_p, C.c_void_p, VP, C.POINTER(D), C.POINTER(D), VP]),
     "tdz_tsurff_destroy": (None, [VP]),
     "tdz_solver_train_coarse": (I, [VP, I, I, C.c_float, C.c_ulonglong, C.POINTER(C.c_float), VP]),
     "tdz_solver_coarse_gain": (I, [VP, I, C.c_ulonglong, C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),

@@ -598,6 +598,44 @@ tdz_status tdz_tsurff_interior(tdz_tsurff *ts, const void *psi, double *out, voi
     });
 }
 
+tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts *inner,
+                               const tdz_tsurff_end_opts *o, const void *psi, double *out, double *stats,
+                               void *stream) {
+    return guarded([&] {
+        TDZ_CHECK(ts && op && psi && out, TDZ_ERR_ARG, "null argument");
+        TDZ_CHECK(reinterpret_cast<uintptr_t>(psi) % 16 == 0, TDZ_ERR_ARG, "psi must be 16-byte aligned");
+        tdz::SolverOptions so;
+        if (inner) {
+            so = solver_options(inner);
+        } else {   // exact banded LU in 1D, fast diagonalisation in 2D/3D (degrees 2..5)
+            const int dim = op->o.sp->dim, p = op->o.sp->ax[0].p;
+            so.pc = dim == 1 ? TDZ_PC_BAND : (p >= 2 && p <= 5 ? TDZ_PC_FDM : TDZ_PC_MASS);
+            so.outer = TDZ_FP64;
+            so.restart = 60;
+        }
+        tdz::EndTermOptions eo;
+        if (o) {
+            eo.dp = o->dp;
+            eo.cap_width = o->cap_width;
+            eo.eta = o->eta;
+            if (o->rtol > 0.0) eo.rtol = o->rtol;
+            if (o->maxit > 0) eo.maxit = o->maxit;
+        }
+        std::vector<tdz::cd> v;
+        const tdz::EndTermStats r = ts->t.end_term(op->o, so, eo, static_cast<const double2 *>(psi), v,
+                                                   static_cast<cudaStream_t>(stream));
+        for (size_t i = 0; i < v.size(); ++i) { out[2 * i] = v[i].real(); out[2 * i + 1] = v[i].imag(); }
+        if (stats) {
+            stats[0] = r.nodes;
+            stats[1] = (double)r.its;
+            stats[2] = r.max_its;
+            stats[3] = r.dp_max;
+            stats[4] = r.eta;
+            stats[5] = r.seconds;
+        }
+    });
+}
+
 tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct) {
     return guarded([&] {
         TDZ_CHECK(ts && abct, TDZ_ERR_ARG, "null argument");

@@ -883,7 +883,7 @@ ZSolveParams line_params(const PcFDM &f) {
     const int dim = f.dim;
     const int *n = f.n;
     const Plan &pl = const_cast<Operator *>(op)->plan(TDZ_STAGE);
-    const std::array<cd, 5> &sg = op->sigma;
+    const std::array<cd, 5> &sg = f.pole ? f.pole_sigma : op->sigma;
     const int outer = dim - 1;
     ZSolveParams zp{};
     zp.ck = f.ufac.as<float2>();

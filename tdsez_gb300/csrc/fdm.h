@@ -35,6 +35,11 @@ struct PcFDM : Precond {
     DevBuf pa, pb;
     int ldx = 0, ldy = 0;
     long long applies = 0;
+    // with `pole`, the line solves use these stage scalars instead of the
+    // operator's (a preconditioner for a shifted copy of the stage, e.g. the
+    // complex-shifted poles of the t-SURFF end term)
+    bool pole = false;
+    std::array<cd, 5> pole_sigma{};
     void setup(Operator *op_);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;
 };

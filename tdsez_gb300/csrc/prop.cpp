@@ -11,6 +11,7 @@
 // (src/propagator.cpp:729-758).
 #include "prop.h"
 
+#include "band.h"
 #include "fdm.h"
 
 #include <cmath>
@@ -60,6 +61,10 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
         pc = std::move(p);
     } else if (o.pc == 3) {
         auto p = std::make_unique<PcFDM>();
+        p->setup(op);
+        pc = std::move(p);
+    } else if (o.pc == 4) {
+        auto p = std::make_unique<PcBand>();
         p->setup(op);
         pc = std::move(p);
     } else throw Error(TDZ_ERR_ARG, "unknown preconditioner");

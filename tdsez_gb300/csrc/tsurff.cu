@@ -330,18 +330,27 @@ void TSurff::advance_volkov(double t) {
     vt = t;
 }
 
-void TSurff::sample(double t, const double2 *psi, cudaStream_t st) {
-    if (have_prev && t == prevT) return;
-    TDZ_CHECK(!have_prev || t > prevT, TDZ_ERR_ARG, "t-SURFF sample times must increase");
-    advance_volkov(t);
+KGridHost TSurff::kgrid() const {
+    KGridHost kg;
+    size_t ka = 0;
+    for (int d = 0; d < 3; ++d) {
+        kg.nk[d] = nk[d];
+        kg.k[d] = kdev.as<double>() + ka;
+        ka += k[d].size();
+    }
+    return kg;
+}
+
+// cur(k) = the surface integral of the flux of psi against the Volkov states
+// at the current Volkov time, before the common factor (FluxGrid)
+void TSurff::surface_flux(const double2 *psi, cudaStream_t st) {
     const double *xw = phase.as<double>();
     size_t xoff[3], woff[3], acc = 0;
     for (int d = 0; d < 3; ++d) { xoff[d] = acc; acc += nodes[d].size(); }
     for (int d = 0; d < 3; ++d) { woff[d] = acc; acc += weights[d].size(); }
-    size_t koff[3], ka = 0;
-    for (int d = 0; d < 3; ++d) { koff[d] = ka; ka += k[d].size(); }
+    const KGridHost kh = kgrid();
     KGrid kg;
-    for (int d = 0; d < 3; ++d) { kg.nk[d] = nk[d]; kg.k[d] = kdev.as<double>() + koff[d]; }
+    for (int d = 0; d < 3; ++d) { kg.nk[d] = kh.nk[d]; kg.k[d] = kh.k[d]; }
     int first = 1;
     for (int a = 0; a < dim; ++a)
         for (int side = 0; side < 2; ++side) {
@@ -378,6 +387,16 @@ void TSurff::sample(double t, const double2 *psi, cudaStream_t st) {
             TDZ_CUDA(cudaGetLastError());
             count_launch(4);
         }
+}
+
+void TSurff::sample(double t, const double2 *psi, cudaStream_t st) {
+    if (have_prev && t == prevT) return;
+    TDZ_CHECK(!have_prev || t > prevT, TDZ_ERR_ARG, "t-SURFF sample times must increase");
+    advance_volkov(t);
+    surface_flux(psi, st);
+    const KGridHost kh = kgrid();
+    KGrid kg;
+    for (int d = 0; d < 3; ++d) { kg.nk[d] = kh.nk[d]; kg.k[d] = kh.k[d]; }
     const double two_pi = 2.0 * std::acos(-1.0);
     const double pref = 0.5 * std::pow(two_pi, -0.5 * dim);
     // pre = (i/2) (2 pi)^{-d/2} exp(i C)
@@ -390,6 +409,47 @@ void TSurff::sample(double t, const double2 *psi, cudaStream_t st) {
     prevT = t;
     have_prev = true;
     ++samples;
+}
+
+namespace {
+// amp[q_e] += w_e pre exp(i (t |k|^2 / 2m + k.B / m)) cur[q_e]; the entries of
+// one node name distinct momenta
+__global__ void k_end_acc(KGrid kg, double2 pre, double t, double inv2m, double invm, double B0, double B1, double B2,
+                          const int *__restrict__ q, const double *__restrict__ w, int m,
+                          const double2 *__restrict__ cur, double2 *__restrict__ amp) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    const size_t idx = (size_t)q[e];
+    int kk[3];
+    kk[2] = (int)(idx % kg.nk[2]);
+    kk[1] = (int)((idx / kg.nk[2]) % kg.nk[1]);
+    kk[0] = (int)(idx / ((size_t)kg.nk[2] * kg.nk[1]));
+    const double Bs[3] = {B0, B1, B2};
+    double phase = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double k = kg.k[d][kk[d]];
+        phase += t * k * k * inv2m + k * Bs[d] * invm;
+    }
+    const double2 c = cmul(cmul(pre, cexpi(phase)), cur[idx]);
+    double2 a = amp[idx];
+    a.x += w[e] * c.x;
+    a.y += w[e] * c.y;
+    amp[idx] = a;
+}
+}  // namespace
+
+void TSurff::add_weighted_flux(const double2 *phi, const int *q, const double *w, int m, cudaStream_t st) {
+    if (m <= 0) return;
+    surface_flux(phi, st);
+    const KGridHost kh = kgrid();
+    KGrid kg;
+    for (int d = 0; d < 3; ++d) { kg.nk[d] = kh.nk[d]; kg.k[d] = kh.k[d]; }
+    const double pref = 0.5 * std::pow(2.0 * std::acos(-1.0), -0.5 * dim);
+    const double2 pre = make_double2(-pref * std::sin(C), pref * std::cos(C));
+    k_end_acc<<<blocks_for((size_t)m), 256, 0, st>>>(kg, pre, vt, 0.5 / mass, 1.0 / mass, B[0], B[1], B[2], q, w, m,
+                                                      cur.as<double2>(), amp_end.as<double2>());
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 namespace {

@@ -8,6 +8,32 @@
 
 namespace tdz {
 
+struct Operator;
+struct SolverOptions;
+
+// momentum grid axes on the device
+struct KGridHost {
+    int nk[3];
+    const double *k[3];
+};
+
+// t-SURFF end term: options and what the run took
+struct EndTermOptions {
+    double dp = 0.0;          // node spacing in |k + A(T)|; 0 = automatic (SurffEndTermDk = 0)
+    double cap_width = 0.0;   // width of the absorbing layer (sets the refined range below 2 k_cap)
+    double eta = -1.0;        // pole damping of the preconditioner: E (1 + i eta); < 0 = automatic
+    double rtol = 1e-10;      // relative residual of every node's solve
+    int maxit = 4000;         // FGMRES iterations per node
+};
+struct EndTermStats {
+    int nodes = 0;            // energy nodes
+    long long its = 0;        // FGMRES iterations over all nodes
+    int max_its = 0;          // largest per node
+    double dp_max = 0.0;      // largest node spacing
+    double eta = 0.0;         // pole damping used
+    double seconds = 0.0;
+};
+
 struct TSurff {
     int dim = 0;
     double R = 0, mass = 1, V0 = 0, sign = 1, dt = 0;
@@ -43,13 +69,28 @@ struct TSurff {
     std::array<std::vector<int>, 3> hoff;
     std::array<std::vector<double>, 3> hval;
     DevBuf F[3], work[2];               // interior projection: per-axis tables and work arrays
+    DevBuf amp_end;                     // end-term amplitudes
+    DevBuf eq, ew;                      // end term: (momentum, weight) entries grouped by node
 
     void setup(const Space &s, const tdz_tsurff_opts &o, tdz_field_fn f, void *ctx);
     // <chi_k(t_last) | theta psi> over the box |x_d| < R (TDSEZTSurff::Interior /
     // Project, src/tsurff.cpp:565-639): out (host) nk complex values, k_x slowest
     void interior(const double2 *psi, std::vector<cd> &out, cudaStream_t st);
     void advance_volkov(double t);
+    KGridHost kgrid() const;
+    // cur = the flux of psi at the current Volkov time without the common factor
+    void surface_flux(const double2 *psi, cudaStream_t st);
     void sample(double t, const double2 *psi, cudaStream_t st);
+    // amp_end[q_e] += w_e flux(phi)(q_e) over m entries (q_e, w_e), the flux at
+    // the last sample with its Volkov factor and no time weight
+    void add_weighted_flux(const double2 *phi, const int *q, const double *w, int m, cudaStream_t st);
+    // The flux after the last sample time T (the field must be over):
+    // sum over energy nodes E_j of Lagrange weights times the flux of
+    // phi_j = (E_j M - H)^-1 i M psi(T), H = op's field-free Hamiltonian with
+    // its absorbing layer (TDSEZTSurff::EndTerm, src/tsurff.cpp:650-976).
+    // out (host): nktot complex amplitudes, k_x slowest.
+    EndTermStats end_term(Operator &op, const SolverOptions &so, const EndTermOptions &eo, const double2 *psi,
+                          std::vector<cd> &out, cudaStream_t st);
 };
 
 }  // namespace tdz

@@ -19,7 +19,8 @@ from . import _lib
 from .operators import Operator
 
 KINDS = {"cn": _lib.TDZ_CN, "pade22": _lib.TDZ_PADE22, "magnus4": _lib.TDZ_MAGNUS4}
-PCS = {"none": _lib.TDZ_PC_NONE, "mass": _lib.TDZ_PC_MASS, "mg": _lib.TDZ_PC_MG, "fdm": _lib.TDZ_PC_FDM}
+PCS = {"none": _lib.TDZ_PC_NONE, "mass": _lib.TDZ_PC_MASS, "mg": _lib.TDZ_PC_MG, "fdm": _lib.TDZ_PC_FDM,
+       "band": _lib.TDZ_PC_BAND}
 S3 = math.sqrt(3.0)
 MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 

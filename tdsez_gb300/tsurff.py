@@ -61,6 +61,30 @@ class TSurff:
                                                    C.c_void_p(s)))
         return out.view(np.complex128)
 
+    def end_term(self, op, psi, cap_width: float = 0.0, dp: float = 0.0, eta: float = -1.0, rtol: float = 1e-10,
+                 maxit: int = 0, inner=None, stream=None):
+        """Flux after the last sample time T of a run that ends after the
+        pulse (``EndTerm``, ``src/tsurff.cpp:650-976``): amplitudes to add to
+        ``amplitudes()``, and a dict of what it took. ``op`` is the field-free
+        Hamiltonian's operator with its absorbing layer, ``psi`` = psi(T)
+        (sampled at T first), ``cap_width`` the layer width
+        (``operators.cap_width(kmin)``; needed when dp = 0), ``inner`` solver
+        options (``propagator.solver_opts``; None: banded LU in 1D, FDM in
+        2D/3D)."""
+        o = _lib.tdz_tsurff_end_opts()
+        o.dp, o.cap_width, o.eta, o.rtol, o.maxit = dp, cap_width, eta, rtol, maxit
+        out = np.zeros(2 * int(np.prod(self.nk)))
+        st = np.zeros(6)
+        inner_p = C.cast(C.byref(inner), C.c_void_p) if inner is not None else None
+        import torch
+        s = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _lib.check(_lib.load().tdz_tsurff_end_term(self.handle, op.handle, inner_p, C.cast(C.byref(o), C.c_void_p),
+                                                   C.c_void_p(psi.data_ptr()), _lib.dptr(out), _lib.dptr(st),
+                                                   C.c_void_p(s)))
+        stats = {"nodes": int(st[0]), "its": int(st[1]), "max_its": int(st[2]), "dp_max": float(st[3]),
+                 "eta": float(st[4]), "seconds": float(st[5])}
+        return out.view(np.complex128), stats
+
     def volkov(self):
         out = np.zeros(8)
         _lib.check(_lib.load().tdz_tsurff_volkov(self.handle, _lib.dptr(out)))

@@ -54,6 +54,23 @@ def _c3():
                 bounds=[(-20.0, 20.0), (-24.0, 24.0)])
 
 
+@case("1d_cap_free")
+def _c1c():
+    """Free carrier in 1D with the absorbing layer (t-SURFF end term)."""
+    p, nq = 4, 6
+    return dict(knots=[ob.uniform_knots(60, -20.0, 20.0, p)], p=p, nq=nq, charge=-1.0, mass=1.0, V=[None],
+                coupled=(0,), cap_kmin=0.5, bounds=[(-20.0, 20.0)])
+
+
+@case("2d_cap_free")
+def _c3c():
+    """Free carrier in 2D with absorbing layers on both axes (t-SURFF end term)."""
+    p, nq = 3, 5
+    knots = [ob.uniform_knots(18, -18.0, 18.0, p), ob.uniform_knots(16, -16.0, 16.0, p)]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, V=[None, None], coupled=(0,), cap_kmin=1.0,
+                bounds=[(-18.0, 18.0), (-16.0, 16.0)])
+
+
 @case("3d_heterostructure")
 def _c4():
     p, nq = 3, 4
