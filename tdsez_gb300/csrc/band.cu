@@ -146,9 +146,9 @@ void PcBand::setup(Operator *op_) {
     lu.alloc((size_t)n * (3 * p + 1) * sizeof(double2));
     piv.alloc((size_t)n * sizeof(int));
     err.alloc(sizeof(int));
-    const size_t smem = (size_t)n * sizeof(double2);
-    if (smem > 48 * 1024)
-        TDZ_CUDA(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the largest vector any instance may stage (the attribute is per kernel, not per launch)
+    TDZ_CUDA(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(kBandMaxRows * sizeof(double2))));
     stale = true;
 }
 
