@@ -101,11 +101,30 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 16;
 
-// C[M][N] (complex) = A[M][K] (complex, lda = K) . B[K][N] (real, ldb = N)
-__global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, const float *__restrict__ B,
+// multiply-accumulate of the transforms: complex data times a real or complex matrix entry
+__device__ __forceinline__ void gmac(float2 &acc, float2 a, float b) {
+    acc.x = fmaf(a.x, b, acc.x);
+    acc.y = fmaf(a.y, b, acc.y);
+}
+__device__ __forceinline__ void gmac(float2 &acc, float a, float2 b) {
+    acc.x = fmaf(a, b.x, acc.x);
+    acc.y = fmaf(a, b.y, acc.y);
+}
+__device__ __forceinline__ void gmac(float2 &acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
+    acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
+}
+template <class T> __device__ __forceinline__ T gzero();
+template <> __device__ __forceinline__ float gzero<float>() { return 0.f; }
+template <> __device__ __forceinline__ float2 gzero<float2>() { return make_float2(0.f, 0.f); }
+
+// C[M][N] (complex) = A[M][K] (complex, row-major) . B[K][N] (real, or complex
+// for complex axis pencils)
+template <class TB>
+__global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, const TB *__restrict__ B,
                                                  float2 *__restrict__ Cm, int M, int N, int K) {
     __shared__ float2 As[BK][BM + 1];
-    __shared__ float Bs[BK][BN + 4];
+    __shared__ TB Bs[BK][BN + 4];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     float2 acc[4][4];
@@ -122,13 +141,13 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
         for (int i = threadIdx.x; i < BK * BN; i += 256) {
             const int k = i / BN, c = i % BN;
             const int gk = k0 + k, gn = n0 + c;
-            Bs[k][c] = (gk < K && gn < N) ? B[(size_t)gk * N + gn] : 0.f;
+            Bs[k][c] = (gk < K && gn < N) ? B[(size_t)gk * N + gn] : gzero<TB>();
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
             float2 a[4];
-            float b[4];
+            TB b[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
 #pragma unroll
@@ -136,10 +155,7 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    acc[r][c].x = fmaf(a[r].x, b[c], acc[r][c].x);
-                    acc[r][c].y = fmaf(a[r].y, b[c], acc[r][c].y);
-                }
+                for (int c = 0; c < 4; ++c) gmac(acc[r][c], a[r], b[c]);
         }
         __syncthreads();
     }
@@ -152,10 +168,12 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
         }
 }
 
-// per plane z: C_z[M][N] (complex) = A[M][K] (real, row-major) . B_z[K][N] (complex)
-__global__ void __launch_bounds__(256) k_gemm_rc(const float *__restrict__ A, const float2 *__restrict__ B,
+// per plane z: C_z[M][N] (complex) = A[M][K] (real, or complex for complex
+// axis pencils; row-major) . B_z[K][N] (complex)
+template <class TA>
+__global__ void __launch_bounds__(256) k_gemm_rc(const TA *__restrict__ A, const float2 *__restrict__ B,
                                                  float2 *__restrict__ Cm, int M, int N, int K) {
-    __shared__ float As[BK][BM + 4];
+    __shared__ TA As[BK][BM + 4];
     __shared__ float2 Bs[BK][BN + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(256) k_gemm_rc(const float *__restrict__ A, co
         for (int i = threadIdx.x; i < BM * BK; i += 256) {
             const int r = i / BK, k = i % BK;
             const int gm = m0 + r, gk = k0 + k;
-            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : 0.f;
+            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : gzero<TA>();
         }
         for (int i = threadIdx.x; i < BK * BN; i += 256) {
             const int k = i / BN, c = i % BN;
@@ -181,7 +199,7 @@ __global__ void __launch_bounds__(256) k_gemm_rc(const float *__restrict__ A, co
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
-            float a[4];
+            TA a[4];
             float2 b[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
@@ -190,10 +208,7 @@ __global__ void __launch_bounds__(256) k_gemm_rc(const float *__restrict__ A, co
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    acc[r][c].x = fmaf(a[r], b[c].x, acc[r][c].x);
-                    acc[r][c].y = fmaf(a[r], b[c].y, acc[r][c].y);
-                }
+                for (int c = 0; c < 4; ++c) gmac(acc[r][c], a[r], b[c]);
         }
         __syncthreads();
     }
@@ -244,6 +259,7 @@ struct ZSolveParams {
     float2 *zb;             // scratch: the band rows of Bc, then of Cc, [2][n2][bw]
     const float *bands;     // outer base bands [nb][n2][bw]
     const float *lx, *ly;   // inner eigenvalues
+    const float *lxi, *lyi; // their imaginary parts (complex axis pencils), else null
     int n0, n1, n2;
     CombP<float> Bc, Cc;    // A_z(s) = Bc + s Cc
 };
@@ -295,7 +311,7 @@ __global__ void k_zbands(const ZSolveParams prm, int bw) {
     }
 }
 
-template <int P>
+template <int P, bool CI>
 __global__ void __launch_bounds__(kZThreads) k_zsolve(const ZSolveParams prm) {
     constexpr int BWd = 2 * P + 1, B = ZBlk<P>::B, NS = ZBlk<P>::NS;
     static_assert(kZDist % B == 0, "row blocks must tile the prefetch ring");
@@ -310,6 +326,7 @@ __global__ void __launch_bounds__(kZThreads) k_zsolve(const ZSolveParams prm) {
     if (l >= nl) return;
     const int i = l % prm.n0, j = l / prm.n0;
     const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
+    const float si = CI ? prm.lxi[i] + (prm.lyi ? prm.lyi[j] : 0.f) : 0.f;
     float *xl = prm.x + (size_t)j * prm.js + (size_t)i * prm.is;
     const size_t ks = prm.ks;
     const int cs = prm.cs;
@@ -335,7 +352,8 @@ __global__ void __launch_bounds__(kZThreads) k_zsolve(const ZSolveParams prm) {
 #pragma unroll
         for (int o = 0; o < BWd; ++o) {
             const float2 b = sB[k * BWd + o], c = sC[k * BWd + o];
-            a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
+            a[o] = CI ? make_float2(fmaf(-si, c.y, fmaf(s, c.x, b.x)), fmaf(si, c.x, fmaf(s, c.y, b.y)))
+                      : make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
         }
 #pragma unroll
         for (int d = P; d >= 1; --d) {
@@ -507,7 +525,7 @@ __host__ __device__ inline int zsolve2_twist(int n2, int B) { return B * ((n2 + 
 
 __device__ __forceinline__ float2 csubf(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 
-template <int P>
+template <int P, bool CI>
 __global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm) {
     constexpr int BWd = 2 * P + 1, B = ZBlk2<P>::B, NS = ZBlk2<P>::NS, T = 2 * kZ2Lines;
     static_assert(kZDist % B == 0, "row blocks must tile the prefetch ring");
@@ -527,6 +545,7 @@ __global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm
     const int L = half ? n - m : m;                // rows of this half
     const int i = l % prm.n0, j = l / prm.n0;
     const float s = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.f);
+    const float si = CI ? prm.lxi[i] + (prm.lyi ? prm.lyi[j] : 0.f) : 0.f;
     float *xl = prm.x + (size_t)j * prm.js + (size_t)i * prm.is;
     const size_t ks = prm.ks;
     const int cs = prm.cs;
@@ -560,7 +579,8 @@ __global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm
         for (int o = 0; o < BWd; ++o) {
             const int oo = half ? 2 * P - o : o;
             const float2 b = sB[pr * BWd + oo], c = sC[pr * BWd + oo];
-            a[o] = make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
+            a[o] = CI ? make_float2(fmaf(-si, c.y, fmaf(s, c.x, b.x)), fmaf(si, c.x, fmaf(s, c.y, b.y)))
+                      : make_float2(fmaf(s, c.x, b.x), fmaf(s, c.y, b.y));
         }
 #pragma unroll
         for (int d = P; d >= 1; --d) {
@@ -774,22 +794,29 @@ __global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm
     }
 }
 
-template <int P> void launch_zsolve(const ZSolveParams &zp, cudaStream_t st) {
+template <int P, bool CI> void launch_zsolve_t(const ZSolveParams &zp, cudaStream_t st) {
     const int nl = zp.n0 * zp.n1;
     k_zbands<<<(zp.n2 * (2 * P + 1) + 255) / 256, 256, 0, st>>>(zp, 2 * P + 1);
     if (zp.n2 >= 4 * ZBlk2<P>::B) {
         const size_t smem = zsolve2_smem<P>(zp.n2);
         TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
         if (smem > 48 * 1024)
-            TDZ_CUDA(cudaFuncSetAttribute(k_zsolve2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_zsolve2<P><<<(nl + kZ2Lines - 1) / kZ2Lines, 2 * kZ2Lines, smem, st>>>(zp);
+            TDZ_CUDA(cudaFuncSetAttribute(k_zsolve2<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_zsolve2<P, CI><<<(nl + kZ2Lines - 1) / kZ2Lines, 2 * kZ2Lines, smem, st>>>(zp);
         return;
     }
     const size_t smem = zsolve_smem<P>(zp.n2);
     TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
     if (smem > 48 * 1024)
-        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_zsolve<P><<<(nl + kZThreads - 1) / kZThreads, kZThreads, smem, st>>>(zp);
+        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_zsolve<P, CI><<<(nl + kZThreads - 1) / kZThreads, kZThreads, smem, st>>>(zp);
+}
+
+// complex eigenvalues (complex axis pencils) take the variant with the
+// imaginary part of the line shift
+template <int P> void launch_zsolve(const ZSolveParams &zp, cudaStream_t st) {
+    if (zp.lxi) launch_zsolve_t<P, true>(zp, st);
+    else launch_zsolve_t<P, false>(zp, st);
 }
 
 // saved-state scratch of the line solves (float2 entries): the larger of the
@@ -831,22 +858,104 @@ void PcFDM::setup(Operator *op_) {
     P = s.ax[0].p;
     TDZ_CHECK(P >= 2 && P <= 5, TDZ_ERR_UNSUPPORTED, "the FDM preconditioner supports degrees 2..5");
     const Plan &pl = op->plan(TDZ_STAGE);
-    // inner one-axis terms must be a common multiple of the stiffness
+    // Inner-axis pencils. With only stiffness on the inner axes the
+    // eigenvectors are those of (S_d, M_d) and the stage factor comes from
+    // the stiffness terms (this also diagonalises stream C). Otherwise, with
+    // no stream C, the pencil is S_d = sum_t f_t B_t over the inner one-axis
+    // terms on the stiffness's stage scalar g (kinetic, potential and
+    // absorbing layer of axis d), with stage factor g: complex symmetric when
+    // the axis has an absorbing layer. Inner terms on other scalars (a field
+    // along an inner axis) are left out of the fast inverse.
     exact = true;
+    pencil = 0;
+    cplx = false;
+    dropped.clear();
     auto pure_s = [&](const Comb &c) {
         for (int i = 0; i < c.n; ++i)
             if (c.base[i] != kS) return false;
         return true;
     };
-    if (pl.hasB && (!pure_s(pl.xT) || (dim == 3 && !pure_s(pl.yT)))) exact = false;
+    const Comb *inner[2] = {&pl.xT, &pl.yT};
+    if (pl.hasB && (!pure_s(pl.xT) || (dim == 3 && !pure_s(pl.yT)))) {
+        if (pl.hasC) {
+            exact = false;
+        } else {
+            pencil = 1;
+            pencil_scalar = -1;
+            for (int t = 0; t < pl.xT.n; ++t)
+                if (pl.xT.base[t] == kS) pencil_scalar = pl.xT.scalar[t];
+            TDZ_CHECK(pencil_scalar >= 0, TDZ_ERR_INTERNAL, "inner axis without a stiffness term");
+            for (int d = 0; d < dim - 1; ++d)
+                for (int t = 0; t < inner[d]->n; ++t)
+                    if (inner[d]->scalar[t] != pencil_scalar) {
+                        exact = false;
+                        dropped.push_back(inner[d]->scalar[t]);
+                    }
+        }
+    }
     if (op->quad.on) exact = false;   // the non-separable term is left out of the fast inverse
     for (int d = 0; d < 3; ++d) n[d] = d < dim ? s.ax[d].n : 1;
     N = (size_t)s.ndof();
-    tensor = dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);
+    // axis pencils: real (S_d, M_d) eigenvectors, or complex ones
+    std::vector<double> Vr[2], lr[2];
+    std::vector<cd> Vc[2], lc[2];
+    bool is_c[2] = {false, false};
     for (int d = 0; d < dim - 1; ++d) {
-        std::vector<double> Vd, ld;
-        gen_eig(op->bases[d][kS], op->bases[d][kM], Vd, ld);
+        if (pencil == 0) {
+            gen_eig(op->bases[d][kS], op->bases[d][kM], Vr[d], lr[d]);
+            continue;
+        }
+        const int bw = 2 * P + 1;
+        std::vector<cd> band((size_t)n[d] * bw, cd(0.0));
+        for (int t = 0; t < inner[d]->n; ++t) {
+            if (inner[d]->scalar[t] != pencil_scalar) continue;
+            const BandD &B = op->bases[d][inner[d]->base[t]];
+            for (size_t e = 0; e < band.size(); ++e) band[e] += inner[d]->factor[t] * B.v[e];
+        }
+        bool imag = false;
+        for (const cd &v : band) imag = imag || v.imag() != 0.0;
+        if (!imag) {
+            BandD re(n[d], P);
+            for (size_t e = 0; e < band.size(); ++e) re.v[e] = band[e].real();
+            gen_eig(re, op->bases[d][kM], Vr[d], lr[d]);
+        } else if (gen_eig_complex(band, P, op->bases[d][kM], Vc[d], lc[d])) {
+            is_c[d] = true;
+        } else {
+            // no complex-orthogonal eigenbasis: fall back to the stiffness pencil
+            pencil = 0;
+            exact = false;
+            dropped.clear();
+            for (int e = 0; e < dim - 1; ++e) {
+                is_c[e] = false;
+                gen_eig(op->bases[e][kS], op->bases[e][kM], Vr[e], lr[e]);
+            }
+            break;
+        }
+    }
+    cplx = is_c[0] || is_c[1];
+    tensor = !cplx && dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);
+    for (int d = 0; d < dim - 1; ++d) {
         const int nd = n[d];
+        if (cplx) {
+            // complex transforms (SIMT): V and V^T as complex FP32, eigenvalues split
+            std::vector<cd> vc = is_c[d] ? Vc[d] : std::vector<cd>(Vr[d].begin(), Vr[d].end());
+            std::vector<cd> l = is_c[d] ? lc[d] : std::vector<cd>(lr[d].begin(), lr[d].end());
+            std::vector<float2> v32((size_t)nd * nd), vt32((size_t)nd * nd);
+            for (int i = 0; i < nd; ++i)
+                for (int j = 0; j < nd; ++j) {
+                    const cd a = vc[(size_t)i * nd + j];
+                    v32[(size_t)i * nd + j] = make_float2((float)a.real(), (float)a.imag());
+                    vt32[(size_t)j * nd + i] = make_float2((float)a.real(), (float)a.imag());
+                }
+            std::vector<float> l32(nd), li32(nd);
+            for (int i = 0; i < nd; ++i) { l32[i] = (float)l[i].real(); li32[i] = (float)l[i].imag(); }
+            upload(V[d], v32);
+            upload(VT[d], vt32);
+            upload(lam[d], l32);
+            upload(lami[d], li32);
+            continue;
+        }
+        const std::vector<double> &Vd = Vr[d], &ld = lr[d];
         std::vector<double> VTd((size_t)nd * nd);
         for (int i = 0; i < nd; ++i)
             for (int j = 0; j < nd; ++j) VTd[(size_t)j * nd + i] = Vd[(size_t)i * nd + j];
@@ -874,6 +983,14 @@ void PcFDM::setup(Operator *op_) {
     }
 }
 
+bool PcFDM::exact_now() const {
+    if (op->quad.on) return false;
+    if (pencil == 0) return exact;
+    for (int sc : dropped)
+        if (op->sigma[sc] != cd(0.0)) return false;
+    return true;
+}
+
 namespace {
 
 // line solve parameters of the current stage (bands and eigenvalues; the
@@ -891,12 +1008,21 @@ ZSolveParams line_params(const PcFDM &f) {
     zp.bands = op->dev32[outer].as<float>();
     zp.lx = f.lam[0].as<float>();
     zp.ly = dim == 3 ? f.lam[1].as<float>() : nullptr;
+    if (f.cplx) {
+        zp.lxi = f.lami[0].as<float>();
+        zp.lyi = dim == 3 ? f.lami[1].as<float>() : nullptr;
+    }
     zp.n0 = n[0];
     zp.n1 = dim == 3 ? n[1] : 1;
     zp.n2 = n[outer];
     zp.Bc = eval_combf(pl.zA, sg);
     Comb cc = pl.zC;
-    if (pl.hasB && pl.xT.n > 0) {
+    if (f.pencil == 1) {
+        // stream B in the eigenbasis: g (lam_x + lam_y) M_out (no stream C)
+        Comb gm;
+        gm.add(kM, f.pencil_scalar, 1.0);
+        zp.Cc = eval_combf(gm, sg);
+    } else if (pl.hasB && pl.xT.n > 0) {
         // stream B: M_out (x) (M_y (x) beta S_x + beta S_y (x) M_x) -> beta M_out
         cd beta = 0.0;
         for (int t = 0; t < pl.xT.n; ++t)
@@ -952,13 +1078,23 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
     float2 *x1 = b1.as<float2>(), *x2 = b2.as<float2>();
     blas::cast(r, TDZ_FP64, x1, TDZ_FP32, N, st);
     const int grows = (int)rows;
+    // transforms along x (rows of n0) and along y (planes of n1 x n0) with a
+    // real or complex FP32 matrix
+    auto along_x = [&](const DevBuf &Mx, const float2 *in, float2 *out) {
+        const dim3 g((n[0] + BN - 1) / BN, (grows + BM - 1) / BM);
+        if (cplx) k_gemm_cr<float2><<<g, 256, 0, st>>>(in, Mx.as<float2>(), out, grows, n[0], n[0]);
+        else k_gemm_cr<float><<<g, 256, 0, st>>>(in, Mx.as<float>(), out, grows, n[0], n[0]);
+    };
+    auto along_y = [&](const DevBuf &My, const float2 *in, float2 *out) {
+        const dim3 g((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]);
+        if (cplx) k_gemm_rc<float2><<<g, 256, 0, st>>>(My.as<float2>(), in, out, n[1], n[0], n[1]);
+        else k_gemm_rc<float><<<g, 256, 0, st>>>(My.as<float>(), in, out, n[1], n[0], n[1]);
+    };
     // forward transforms: along x with V (t_i = sum_i' V[i'][i] r_i'), along y with V^T
-    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (grows + BM - 1) / BM), 256, 0, st>>>(x1, V[0].as<float>(), x2, grows, n[0],
-                                                                                 n[0]);
+    along_x(V[0], x1, x2);
     float2 *cur = x2, *oth = x1;
     if (dim == 3) {
-        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(VT[1].as<float>(), x2, x1,
-                                                                                        n[1], n[0], n[1]);
+        along_y(VT[1], x2, x1);
         cur = x1;
         oth = x2;
     }
@@ -973,12 +1109,10 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
     line_solve(P, zp, st);
     // inverse transforms: along y with V, along x with V^T
     if (dim == 3) {
-        k_gemm_rc<<<dim3((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]), 256, 0, st>>>(V[1].as<float>(), cur, oth,
-                                                                                        n[1], n[0], n[1]);
+        along_y(V[1], cur, oth);
         std::swap(cur, oth);
     }
-    k_gemm_cr<<<dim3((n[0] + BN - 1) / BN, (grows + BM - 1) / BM), 256, 0, st>>>(cur, VT[0].as<float>(), oth, grows,
-                                                                                 n[0], n[0]);
+    along_x(VT[0], cur, oth);
     TDZ_CUDA(cudaGetLastError());
     count_launch(dim == 3 ? 4 : 2);
     blas::cast(oth, TDZ_FP32, z, TDZ_FP64, N, st);

@@ -12,6 +12,10 @@ namespace tdz {
 // Generalised symmetric eigenproblem S V = M V diag(lam), V^T M V = I
 // (dense, host, FP64; Cholesky reduction + cyclic Jacobi).
 void gen_eig(const BandD &S, const BandD &M, std::vector<double> &V, std::vector<double> &lam);
+// The same for a complex symmetric band S ([n][2p+1]) against the real SPD M:
+// S V = M V diag(lam), V^T M V = I (bilinear, not Hermitian). Returns false
+// when no such basis is found to working accuracy (eig_cs.cpp).
+bool gen_eig_complex(const std::vector<cd> &S, int p, const BandD &M, std::vector<cd> &V, std::vector<cd> &lam);
 
 // A = (M_x (x) M_y) (x) Bz + (S_x (x) M_y + M_x (x) S_y) (x) Cz with Bz, Cz
 // combinations of the outer-axis base bands. Then
@@ -24,10 +28,22 @@ struct PcFDM : Precond {
     int n[3] = {1, 1, 1};
     size_t N = 0;
     DevBuf V[2], VT[2];        // FP32 n_d x n_d (row-major) eigenvectors and their transpose
+                               // (complex FP32 when cplx)
     DevBuf lam[2];             // FP32 eigenvalues per inner axis
+    DevBuf lami[2];            // their imaginary parts (cplx)
+    // inner-axis pencils: 0 = stiffness only; 1 = S_d = all inner one-axis
+    // terms on the common stage scalar pencil_scalar (exact for operators with
+    // potentials and absorbing layers on the inner axes, no field there)
+    int pencil = 0, pencil_scalar = 1;
+    bool cplx = false;         // some axis pencil is complex symmetric (absorbing layer)
+    std::vector<int> dropped;  // stage scalars of inner terms left out of the pencil (pencil 1)
+    // the inverse is exact (to FP32) for the operator's current stage: nothing
+    // dropped, or the dropped terms' stage scalars are zero now
+    bool exact_now() const;
     DevBuf zb;                 // FP32 band rows of the line matrices, Bc then Cc, [2][n_outer][2P+1]
     DevBuf b1, b2, ufac;       // FP32 work vectors and the saved elimination states of the line solves
-    bool exact = true;         // false: inner one-axis terms other than stiffness were dropped
+    bool exact = true;         // false: inner one-axis terms were dropped (stiffness-only pencil, or a
+                               // field along an inner axis)
     // 3D with n_x, n_y <= 256: transforms on the tensor cores (tcgen05, TF32 hi/lo split) over
     // row-planar FP32 buffers pa ([z][y][c][x], pitch ldx) and pb ([z][x][c][y], pitch ldy)
     bool tensor = false;

@@ -14,10 +14,12 @@
 // The reference runs a multi-shift Arnoldi on LU-factorised (or ASM/GMRES)
 // poles. Here every node is its own FGMRES solve on the device, warm-started
 // from the previous node's solution, with the library's preconditioners:
-// the exact banded LU in 1D, the fast-diagonalisation inverse in 2D/3D. When
-// that inverse is not exact (absorbing layers along the inner axes), it is
-// built for the damped pole E (1 + i eta) (the shifted-Laplacian rule the
-// reference uses for its 3D poles) while FGMRES solves the undamped system.
+// the exact banded LU in 1D, the fast-diagonalisation inverse in 2D/3D
+// (exact for a separable H: its absorbing layers enter through complex
+// symmetric axis pencils). When that inverse is not exact (a non-separable
+// potential), it is built for the damped pole E (1 + i eta) (the
+// shifted-Laplacian rule the reference uses for its 3D poles) while FGMRES
+// solves the undamped system.
 // The flux of a node is added to the momenta that use it as soon as it is
 // solved, so no node solution is kept.
 #include <algorithm>
@@ -157,7 +159,7 @@ EndTermStats TSurff::end_term(Operator &op, const SolverOptions &so_in, const En
     auto *fdm = so.pc == TDZ_PC_FDM ? static_cast<PcFDM *>(sol.pc.get()) : nullptr;
     auto *band = so.pc == TDZ_PC_BAND ? static_cast<PcBand *>(sol.pc.get()) : nullptr;
     double eta = eo.eta;
-    if (eta < 0.0) eta = (fdm && !fdm->exact) || (band && !band->exact) ? 0.5 : 0.0;
+    if (eta < 0.0) eta = (fdm && !fdm->exact_now()) || (band && !band->exact) ? 0.5 : 0.0;
 
     EndTermStats stats;
     stats.nodes = nn;

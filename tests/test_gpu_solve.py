@@ -89,6 +89,44 @@ def test_fdm_solve(cuda, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name,cc", [("2d_cap_free", [0.0]), ("2d_cap_softcore_sep", [0.0]),
+                                     ("3d_const_mass_cap", [0.0, 0.03])])
+def test_fdm_complex_pencils(cuda, name, cc):
+    """Absorbing layers (and separable potentials) on the inner axes enter the
+    fast-diagonalisation inverse through complex symmetric axis pencils
+    S_d = K_d + V_d - i W_d with V^T M V = I: with no field along an inner
+    axis the inverse is exact to FP32, so FGMRES needs one digit group per
+    iteration, and reaches the direct solution."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    tau = 0.2
+    op.set_stage(1.0, 1j * tau, cc)
+    Am = (A.M + 1j * tau * (A.H_total() + sum(ck * T for ck, T in zip(cc, A.terms())))).tocsc()
+    rng = np.random.default_rng(9)
+    b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    s = Solver(op, pc="fdm", precision="fp32", rtol=1e-12, maxit=100)
+    bd = torch.tensor(b, device=cuda)
+    xd = torch.zeros_like(bd)
+    its, reason, rn = s.solve(bd, xd)
+    x = xd.cpu().numpy()
+    assert reason > 0, (its, reason, rn)
+    assert _berr(Am, x, b) < 1e-12, _berr(Am, x, b)
+    assert its <= 4, its
+    # the end term's indefinite stage E M - H as well
+    E = 0.6
+    op.set_stage(E, -1.0, [0.0] * len(cc))
+    Ah = (E * A.M - A.H_total()).tocsc()
+    xref = sla.spsolve(Ah, b)
+    xd.zero_()
+    its, reason, rn = s.solve(bd, xd)
+    assert reason > 0 and its <= 6, (its, reason)
+    assert _rel(xd.cpu().numpy(), xref) < 1e-9
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("p,nel_z", [(2, 62), (2, 80), (3, 29), (3, 45), (3, 61), (4, 40), (5, 33), (5, 57)])
 def test_fdm_line_solve_lengths(cuda, p, nel_z):
     """FDM inverse on z-layered operators with long z axes (the two-thread line

@@ -105,6 +105,9 @@ def test_end_term_parity(cuda, name, R, kg, dp):
     out, stats = gpu.end_term(op, torch.tensor(st, device=cuda), cap_width=width, dp=dp, rtol=1e-11)
     print(f"{name}: {stats}")
     assert stats["nodes"] == len(nodes)
+    # exact preconditioners: the banded LU (1D) and the FDM inverse with
+    # complex symmetric axis pencils (2D), so a few iterations per node
+    assert stats["eta"] == 0.0 and stats["max_its"] <= 6, stats
     err = np.abs(out - ref).max() / np.abs(ref).max()
     assert err < 1e-8, err
     # the flux part is unchanged by the end term
@@ -145,6 +148,40 @@ def test_end_term_end1d_on_the_gpu(cuda):
     assert abs(np.trapezoid(pes, ks) - 1.0) < 1e-3
     assert abs(np.trapezoid(np.abs(amp) ** 2, ks) - 1.0) > 0.2
     assert stats["nodes"] > 50
+
+
+@pytest.mark.gpu
+def test_end_term_end2d_on_the_gpu(cuda):
+    """2D deck of the reference's end-term test (p = 4, 56 x 56 elements on
+    [-20, 20]^2, CAP k_min 1, CN dt 0.02 to T = 2, packet k0 = (2, 1), R = 6,
+    31 x 31 momenta on [-1, 5] x [-2, 4], no field): the packet is still inside
+    the box at T; flux plus end term give the analytic spectrum to 1e-2."""
+    import torch
+    from oracle import bspline as ob
+    from tdsez_gb300.operators import Operator, Physics, cap_width
+    from tdsez_gb300.propagator import Propagator
+    from tdsez_gb300.space import Space
+    from tdsez_gb300.tsurff import TSurff
+    p, L = 4, 20.0
+    kn = ob.uniform_knots(56, -L, L, p)
+    PS = Space([kn, kn], p, 6)
+    op = Operator(PS, Physics(cap_kmin=1.0, bounds=[(-L, L), (-L, L)], coupled=(0,)))
+    w, k0 = 1.0, (2.0, 1.0)
+    psi = op.separable_state([lambda x, k=k: (2 * np.pi * w * w) ** -0.25 * np.exp(-x * x / (4 * w * w) + 1j * k * x)
+                              for k in k0])
+    fld = lambda t: [0.0, 0.0]
+    G = Propagator(op, "cn", field=fld, pc="fdm", precision="fp32", rtol=1e-12, guess_order=-1)
+    ts = TSurff(PS, 6.0, [(-1.0, 5.0, 31), (-2.0, 4.0, 31)], fld, 0.02)
+    G.evolve(psi, 0.02, 2.0, monitor=lambda step, t, ps: ts.sample(t, ps))
+    end, stats = ts.end_term(op, psi, cap_width=cap_width(1.0))
+    print(stats)
+    b = (ts.amplitudes() + end).reshape(31, 31)
+    kx, ky = np.linspace(-1, 5, 31), np.linspace(-2, 4, 31)
+    ex = np.outer((2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (kx - k0[0]) ** 2),
+                  (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ky - k0[1]) ** 2))
+    err = np.abs(np.abs(b) ** 2 - ex).max() / ex.max()
+    assert err < 1e-2, err
+    assert stats["max_its"] <= 8, stats
 
 
 @pytest.mark.gpu
