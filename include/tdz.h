@@ -180,9 +180,14 @@ typedef struct tdz_solver tdz_solver;
 #define TDZ_PC_NONE 0
 #define TDZ_PC_MASS 1 /* exact Kronecker inverse of the overlap M           */
 #define TDZ_PC_MG 2   /* geometric B-spline multigrid V-cycle               */
-#define TDZ_PC_FDM 3  /* fast diagonalisation: exact FP32 inverse of operators
-                         whose inner axes carry only mass and stiffness (the
-                         z-layered structure), approximate otherwise          */
+#define TDZ_PC_FDM 3  /* fast diagonalisation: exact inverse (FP32, or FP64
+                         with pc_precision = TDZ_FP64) of separable
+                         operators: inner axes with only mass and stiffness
+                         (the z-layered structure), or, with a constant mass,
+                         inner-axis potentials and absorbing layers (complex
+                         symmetric axis pencils); terms of other stage
+                         scalars on the inner axes (a field along them) and
+                         non-separable potentials are left out             */
 #define TDZ_PC_BAND 4 /* 1D: exact banded LU with partial pivoting (FP64) of
                          the stage operator, refactored when the refresh rule
                          asks (tdz_pc_refresh_stale) or the end term moves to
@@ -446,13 +451,14 @@ tdz_status tdz_tsurff_interior(tdz_tsurff *ts, const void *psi, double *out, voi
  * largest box half-width) and the node fluxes are combined with four-point
  * Lagrange weights in p. Every node is one FGMRES solve (FP64, relative
  * residual rtol) on the device, warm-started from the previous node, with
- * the preconditioner of `inner` (NULL: the exact banded LU in 1D, the FDM
- * inverse in 2D/3D, built for the damped pole E (1 + i eta) when it is not
- * exact). psi: psi(T) (FP64 device vector), sampled at T before the call.
- * out (host): prod(nk) complex values, k_x slowest, to be added to
- * tdz_tsurff_amplitudes. stats (host, may be NULL, 6 doubles): nodes, total
- * FGMRES iterations, largest per node, largest node spacing, eta used,
- * seconds. Fails (TDZ_ERR_ARG) when the field is not over at T. The
+ * the preconditioner of `inner` (NULL: the exact banded LU in 1D, the FP64
+ * FDM inverse in 2D/3D, built for the damped pole E (1 + i eta) when it is not
+ * exact; an exact FP32 inverse that stagnates at a nearly singular node is
+ * replaced by the damped pole for that node). psi: psi(T) (FP64 device
+ * vector), sampled at T before the call. out (host): prod(nk) complex
+ * values, k_x slowest, to be added to tdz_tsurff_amplitudes. stats (host,
+ * may be NULL, 7 doubles): nodes, total FGMRES iterations, largest per node,
+ * largest node spacing, eta used, seconds, nodes that needed the damped pole. Fails (TDZ_ERR_ARG) when the field is not over at T. The
  * operator's stage coefficients are overwritten. */
 typedef struct tdz_tsurff_end_opts {
     double dp;          /* node spacing in p (SurffEndTermDk); 0 = automatic  */

@@ -610,6 +610,10 @@ tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts
         } else {   // exact banded LU in 1D, fast diagonalisation in 2D/3D (degrees 2..5)
             const int dim = op->o.sp->dim, p = op->o.sp->ax[0].p;
             so.pc = dim == 1 ? TDZ_PC_BAND : (p >= 2 && p <= 5 ? TDZ_PC_FDM : TDZ_PC_MASS);
+            // FP64: the complex eigenbases of absorbing layers can be far from
+            // orthogonal, and nodes next to weakly absorbed box modes are
+            // nearly singular; an FP32 inverse loses every digit there
+            so.pc_precision = TDZ_FP64;
             so.outer = TDZ_FP64;
             so.restart = 60;
         }
@@ -632,6 +636,7 @@ tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts
             stats[3] = r.dp_max;
             stats[4] = r.eta;
             stats[5] = r.seconds;
+            stats[6] = r.damped;
         }
     });
 }

@@ -101,42 +101,51 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 16;
 
-// multiply-accumulate of the transforms: complex data times a real or complex matrix entry
-__device__ __forceinline__ void gmac(float2 &acc, float2 a, float b) {
-    acc.x = fmaf(a.x, b, acc.x);
-    acc.y = fmaf(a.y, b, acc.y);
+// multiply-accumulate of the transforms: complex data times a real or complex
+// matrix entry (FP32, or FP64 for the FP64 preconditioner)
+template <class C, class R> __device__ __forceinline__ void gmac(C &acc, C a, R b) {
+    acc.x = fma(a.x, b, acc.x);
+    acc.y = fma(a.y, b, acc.y);
 }
-__device__ __forceinline__ void gmac(float2 &acc, float a, float2 b) {
-    acc.x = fmaf(a, b.x, acc.x);
-    acc.y = fmaf(a, b.y, acc.y);
+template <class C, class R> __device__ __forceinline__ void gmac_r(C &acc, R a, C b) {
+    acc.x = fma(a, b.x, acc.x);
+    acc.y = fma(a, b.y, acc.y);
 }
-__device__ __forceinline__ void gmac(float2 &acc, float2 a, float2 b) {
-    acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
-    acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
+template <class C> __device__ __forceinline__ void gmac_c(C &acc, C a, C b) {
+    acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+    acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
 }
+__device__ __forceinline__ void gmac2(float2 &acc, float2 a, float b) { gmac(acc, a, b); }
+__device__ __forceinline__ void gmac2(float2 &acc, float a, float2 b) { gmac_r(acc, a, b); }
+__device__ __forceinline__ void gmac2(float2 &acc, float2 a, float2 b) { gmac_c(acc, a, b); }
+__device__ __forceinline__ void gmac2(double2 &acc, double2 a, double b) { gmac(acc, a, b); }
+__device__ __forceinline__ void gmac2(double2 &acc, double a, double2 b) { gmac_r(acc, a, b); }
+__device__ __forceinline__ void gmac2(double2 &acc, double2 a, double2 b) { gmac_c(acc, a, b); }
 template <class T> __device__ __forceinline__ T gzero();
 template <> __device__ __forceinline__ float gzero<float>() { return 0.f; }
 template <> __device__ __forceinline__ float2 gzero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double gzero<double>() { return 0.0; }
+template <> __device__ __forceinline__ double2 gzero<double2>() { return make_double2(0.0, 0.0); }
 
-// C[M][N] (complex) = A[M][K] (complex, row-major) . B[K][N] (real, or complex
-// for complex axis pencils)
-template <class TB>
-__global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, const TB *__restrict__ B,
-                                                 float2 *__restrict__ Cm, int M, int N, int K) {
-    __shared__ float2 As[BK][BM + 1];
+// C[M][N] (complex C2) = A[M][K] (complex, row-major) . B[K][N] (real, or
+// complex for complex axis pencils)
+template <class C2, class TB>
+__global__ void __launch_bounds__(256) k_gemm_cr(const C2 *__restrict__ A, const TB *__restrict__ B,
+                                                 C2 *__restrict__ Cm, int M, int N, int K) {
+    __shared__ C2 As[BK][BM + 1];
     __shared__ TB Bs[BK][BN + 4];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    float2 acc[4][4];
+    C2 acc[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < 4; ++c) acc[r][c] = gzero<C2>();
     for (int k0 = 0; k0 < K; k0 += BK) {
         for (int i = threadIdx.x; i < BM * BK; i += 256) {
             const int r = i / BK, k = i % BK;
             const int gm = m0 + r, gk = k0 + k;
-            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : make_float2(0.f, 0.f);
+            As[k][r] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : gzero<C2>();
         }
         for (int i = threadIdx.x; i < BK * BN; i += 256) {
             const int k = i / BN, c = i % BN;
@@ -146,7 +155,7 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
-            float2 a[4];
+            C2 a[4];
             TB b[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
@@ -155,7 +164,7 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) gmac(acc[r][c], a[r], b[c]);
+                for (int c = 0; c < 4; ++c) gmac2(acc[r][c], a[r], b[c]);
         }
         __syncthreads();
     }
@@ -168,23 +177,23 @@ __global__ void __launch_bounds__(256) k_gemm_cr(const float2 *__restrict__ A, c
         }
 }
 
-// per plane z: C_z[M][N] (complex) = A[M][K] (real, or complex for complex
-// axis pencils; row-major) . B_z[K][N] (complex)
-template <class TA>
-__global__ void __launch_bounds__(256) k_gemm_rc(const TA *__restrict__ A, const float2 *__restrict__ B,
-                                                 float2 *__restrict__ Cm, int M, int N, int K) {
+// per plane z: C_z[M][N] (complex C2) = A[M][K] (real, or complex for
+// complex axis pencils; row-major) . B_z[K][N] (complex)
+template <class C2, class TA>
+__global__ void __launch_bounds__(256) k_gemm_rc(const TA *__restrict__ A, const C2 *__restrict__ B,
+                                                 C2 *__restrict__ Cm, int M, int N, int K) {
     __shared__ TA As[BK][BM + 4];
-    __shared__ float2 Bs[BK][BN + 1];
+    __shared__ C2 Bs[BK][BN + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const size_t plane = (size_t)blockIdx.z;
-    const float2 *Bz = B + plane * (size_t)K * N;
-    float2 *Cz = Cm + plane * (size_t)M * N;
-    float2 acc[4][4];
+    const C2 *Bz = B + plane * (size_t)K * N;
+    C2 *Cz = Cm + plane * (size_t)M * N;
+    C2 acc[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < 4; ++c) acc[r][c] = gzero<C2>();
     for (int k0 = 0; k0 < K; k0 += BK) {
         for (int i = threadIdx.x; i < BM * BK; i += 256) {
             const int r = i / BK, k = i % BK;
@@ -194,13 +203,13 @@ __global__ void __launch_bounds__(256) k_gemm_rc(const TA *__restrict__ A, const
         for (int i = threadIdx.x; i < BK * BN; i += 256) {
             const int k = i / BN, c = i % BN;
             const int gk = k0 + k, gn = n0 + c;
-            Bs[k][c] = (gk < K && gn < N) ? Bz[(size_t)gk * N + gn] : make_float2(0.f, 0.f);
+            Bs[k][c] = (gk < K && gn < N) ? Bz[(size_t)gk * N + gn] : gzero<C2>();
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
             TA a[4];
-            float2 b[4];
+            C2 b[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) a[r] = As[k][ty * 4 + r];
 #pragma unroll
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(256) k_gemm_rc(const TA *__restrict__ A, const
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) gmac(acc[r][c], a[r], b[c]);
+                for (int c = 0; c < 4; ++c) gmac2(acc[r][c], a[r], b[c]);
         }
         __syncthreads();
     }
@@ -836,22 +845,12 @@ size_t zsolve_state_size(int P, int n2, size_t lines) {
     }
 }
 
-CombP<float> eval_combf(const Comb &c, const std::array<cd, 5> &sg, cd extra_scale = 1.0) {
-    CombP<float> out{};
-    out.n = c.n;
-    for (int i = 0; i < c.n; ++i) {
-        const cd v = c.factor[i] * sg[c.scalar[i]] * extra_scale;
-        out.base[i] = c.base[i];
-        out.re[i] = (float)v.real();
-        out.im[i] = (float)v.imag();
-    }
-    return out;
-}
-
 }  // namespace
 
-void PcFDM::setup(Operator *op_) {
+void PcFDM::setup(Operator *op_, int prec) {
     op = op_;
+    TDZ_CHECK(prec == TDZ_FP32 || prec == TDZ_FP64, TDZ_ERR_ARG, "FDM precision must be FP32 or FP64");
+    f64 = prec == TDZ_FP64;
     const Space &s = *op->sp;
     dim = s.dim;
     TDZ_CHECK(dim >= 2, TDZ_ERR_UNSUPPORTED, "the FDM preconditioner needs 2D or 3D");
@@ -933,42 +932,59 @@ void PcFDM::setup(Operator *op_) {
         }
     }
     cplx = is_c[0] || is_c[1];
-    tensor = !cplx && dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);
+    tensor = !f64 && !cplx && dim == 3 && transform_supported(n[0]) && transform_supported(n[1]);
+    // transform matrices and eigenvalues in the preconditioner's precision
+    auto up = [&](DevBuf &b, const std::vector<double> &v) {
+        if (f64) upload(b, v);
+        else upload(b, std::vector<float>(v.begin(), v.end()));
+    };
+    auto upc = [&](DevBuf &b, const std::vector<cd> &v) {
+        if (f64) {
+            std::vector<double2> h(v.size());
+            for (size_t e = 0; e < v.size(); ++e) h[e] = make_double2(v[e].real(), v[e].imag());
+            upload(b, h);
+        } else {
+            std::vector<float2> h(v.size());
+            for (size_t e = 0; e < v.size(); ++e) h[e] = make_float2((float)v[e].real(), (float)v[e].imag());
+            upload(b, h);
+        }
+    };
     for (int d = 0; d < dim - 1; ++d) {
         const int nd = n[d];
         if (cplx) {
-            // complex transforms (SIMT): V and V^T as complex FP32, eigenvalues split
-            std::vector<cd> vc = is_c[d] ? Vc[d] : std::vector<cd>(Vr[d].begin(), Vr[d].end());
-            std::vector<cd> l = is_c[d] ? lc[d] : std::vector<cd>(lr[d].begin(), lr[d].end());
-            std::vector<float2> v32((size_t)nd * nd), vt32((size_t)nd * nd);
+            // complex transforms (SIMT): V and V^T complex, eigenvalues split into parts
+            const std::vector<cd> vc = is_c[d] ? Vc[d] : std::vector<cd>(Vr[d].begin(), Vr[d].end());
+            const std::vector<cd> l = is_c[d] ? lc[d] : std::vector<cd>(lr[d].begin(), lr[d].end());
+            std::vector<cd> vt((size_t)nd * nd);
             for (int i = 0; i < nd; ++i)
-                for (int j = 0; j < nd; ++j) {
-                    const cd a = vc[(size_t)i * nd + j];
-                    v32[(size_t)i * nd + j] = make_float2((float)a.real(), (float)a.imag());
-                    vt32[(size_t)j * nd + i] = make_float2((float)a.real(), (float)a.imag());
-                }
-            std::vector<float> l32(nd), li32(nd);
-            for (int i = 0; i < nd; ++i) { l32[i] = (float)l[i].real(); li32[i] = (float)l[i].imag(); }
-            upload(V[d], v32);
-            upload(VT[d], vt32);
-            upload(lam[d], l32);
-            upload(lami[d], li32);
+                for (int j = 0; j < nd; ++j) vt[(size_t)j * nd + i] = vc[(size_t)i * nd + j];
+            std::vector<double> lre(nd), lim(nd);
+            for (int i = 0; i < nd; ++i) { lre[i] = l[i].real(); lim[i] = l[i].imag(); }
+            upc(V[d], vc);
+            upc(VT[d], vt);
+            up(lam[d], lre);
+            up(lami[d], lim);
             continue;
         }
         const std::vector<double> &Vd = Vr[d], &ld = lr[d];
         std::vector<double> VTd((size_t)nd * nd);
         for (int i = 0; i < nd; ++i)
             for (int j = 0; j < nd; ++j) VTd[(size_t)j * nd + i] = Vd[(size_t)i * nd + j];
-        std::vector<float> v32(Vd.begin(), Vd.end()), vt32(VTd.begin(), VTd.end()), l32(ld.begin(), ld.end());
-        upload(lam[d], l32);
+        up(lam[d], ld);
         if (tensor) {
             // 3D: eigenvector transforms on the tensor cores (forward with V, inverse with V^T)
             Tf[d].build(Vd, nd, nd);
             Ti[d].build(VTd, nd, nd);
         } else {
-            upload(V[d], v32);
-            upload(VT[d], vt32);
+            up(V[d], Vd);
+            up(VT[d], VTd);
         }
+    }
+    if (f64) {
+        ufac.alloc(N * (P + 1) * sizeof(double2));
+        b1.alloc(N * sizeof(double2));
+        b2.alloc(N * sizeof(double2));
+        return;
     }
     ufac.alloc(zsolve_state_size(P, n[dim - 1], N / n[dim - 1]) * sizeof(float2));
     zb.alloc((size_t)2 * n[dim - 1] * (2 * P + 1) * sizeof(float2));
@@ -995,12 +1011,49 @@ namespace {
 
 // line solve parameters of the current stage (bands and eigenvalues; the
 // caller sets the data layout)
+// stage coefficients of the line matrices A_z(s) = Bc + s Cc of the current
+// (or pole) stage, as CombP of the precision T
+template <class T> void line_combs(const PcFDM &f, CombP<T> &Bc, CombP<T> &Cc) {
+    const Operator *op = f.op;
+    const Plan &pl = const_cast<Operator *>(op)->plan(TDZ_STAGE);
+    const std::array<cd, 5> &sg = f.pole ? f.pole_sigma : op->sigma;
+    auto eval = [&](const Comb &c) {
+        CombP<T> out{};
+        out.n = c.n;
+        for (int i = 0; i < c.n; ++i) {
+            const cd v = c.factor[i] * sg[c.scalar[i]];
+            out.base[i] = c.base[i];
+            out.re[i] = (T)v.real();
+            out.im[i] = (T)v.imag();
+        }
+        return out;
+    };
+    Bc = eval(pl.zA);
+    Comb cc = pl.zC;
+    if (f.pencil == 1) {
+        // stream B in the eigenbasis: g (lam_x + lam_y) M_out (no stream C)
+        Comb gm;
+        gm.add(kM, f.pencil_scalar, 1.0);
+        Cc = eval(gm);
+    } else if (pl.hasB && pl.xT.n > 0) {
+        // stream B: M_out (x) (M_y (x) beta S_x + beta S_y (x) M_x) -> beta M_out
+        cd beta = 0.0;
+        for (int t = 0; t < pl.xT.n; ++t)
+            if (pl.xT.base[t] == kS) beta += pl.xT.factor[t] * sg[pl.xT.scalar[t]];
+        cc.add(kM, 0, 0.0);
+        CombP<T> c = eval(cc);
+        for (int t = 0; t < c.n; ++t)
+            if (c.base[t] == kM) { c.re[t] += (T)beta.real(); c.im[t] += (T)beta.imag(); }
+        Cc = c;
+    } else {
+        Cc = eval(cc);
+    }
+}
+
 ZSolveParams line_params(const PcFDM &f) {
     const Operator *op = f.op;
     const int dim = f.dim;
     const int *n = f.n;
-    const Plan &pl = const_cast<Operator *>(op)->plan(TDZ_STAGE);
-    const std::array<cd, 5> &sg = f.pole ? f.pole_sigma : op->sigma;
     const int outer = dim - 1;
     ZSolveParams zp{};
     zp.ck = f.ufac.as<float2>();
@@ -1015,27 +1068,108 @@ ZSolveParams line_params(const PcFDM &f) {
     zp.n0 = n[0];
     zp.n1 = dim == 3 ? n[1] : 1;
     zp.n2 = n[outer];
-    zp.Bc = eval_combf(pl.zA, sg);
-    Comb cc = pl.zC;
-    if (f.pencil == 1) {
-        // stream B in the eigenbasis: g (lam_x + lam_y) M_out (no stream C)
-        Comb gm;
-        gm.add(kM, f.pencil_scalar, 1.0);
-        zp.Cc = eval_combf(gm, sg);
-    } else if (pl.hasB && pl.xT.n > 0) {
-        // stream B: M_out (x) (M_y (x) beta S_x + beta S_y (x) M_x) -> beta M_out
-        cd beta = 0.0;
-        for (int t = 0; t < pl.xT.n; ++t)
-            if (pl.xT.base[t] == kS) beta += pl.xT.factor[t] * sg[pl.xT.scalar[t]];
-        cc.add(kM, 0, 0.0);
-        CombP<float> c = eval_combf(cc, sg);
-        for (int t = 0; t < c.n; ++t)
-            if (c.base[t] == kM) { c.re[t] += (float)beta.real(); c.im[t] += (float)beta.imag(); }
-        zp.Cc = c;
-    } else {
-        zp.Cc = eval_combf(cc, sg);
-    }
+    line_combs<float>(f, zp.Bc, zp.Cc);
     return zp;
+}
+
+// FP64 line solves (the FP64 preconditioner): one thread per line, banded LU
+// without pivoting as in the FP32 solves, the U rows kept in a global
+// scratch, the line matrices evaluated from the FP64 bands row by row
+struct Line64Params {
+    double2 *x;               // line (i, j), row k at x[k ks + j js + i]
+    size_t ks;
+    int js;
+    int n0, n1, n2;
+    const double *bands;      // outer base bands [nb][n2][2P+1] (FP64)
+    const double *lx, *ly, *lxi, *lyi;
+    CombP<double> Bc, Cc;
+    double2 *U;               // [n2][P + 1][lines]: reciprocal pivot, then the upper band
+};
+
+template <int P> __global__ void __launch_bounds__(128) k_line64(const Line64Params prm) {
+    constexpr int BW = 2 * P + 1;
+    const int nl = prm.n0 * prm.n1;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nl) return;
+    const int i = l % prm.n0, j = l / prm.n0;
+    const double sr = prm.lx[i] + (prm.ly ? prm.ly[j] : 0.0);
+    const double si = (prm.lxi ? prm.lxi[i] : 0.0) + (prm.lyi ? prm.lyi[j] : 0.0);
+    double2 *xl = prm.x + (size_t)j * prm.js + i;
+    const int n = prm.n2;
+    const size_t ks = prm.ks;
+    auto U = [&](int k, int q) -> double2 & { return prm.U[((size_t)k * (P + 1) + q) * nl + l]; };
+    auto cm = [](double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+    for (int k = 0; k < n; ++k) {
+        double2 a[BW];
+#pragma unroll
+        for (int o = 0; o < BW; ++o) {
+            const double2 b = comb_at<double, double2>(prm.Bc, prm.bands, n, BW, k, o);
+            const double2 c = comb_at<double, double2>(prm.Cc, prm.bands, n, BW, k, o);
+            a[o] = make_double2(b.x + sr * c.x - si * c.y, b.y + sr * c.y + si * c.x);
+        }
+        double2 rhs = xl[(size_t)k * ks];
+#pragma unroll
+        for (int d = P; d >= 1; --d) {
+            const int r = k - d;
+            if (r < 0) continue;
+            const double2 f = cm(a[P - d], U(r, 0));
+#pragma unroll
+            for (int q = 1; q <= P; ++q) {
+                if (P - d + q >= BW) break;
+                const double2 u = cm(f, U(r, q));
+                a[P - d + q].x -= u.x;
+                a[P - d + q].y -= u.y;
+            }
+            const double2 y = cm(f, xl[(size_t)r * ks]);
+            rhs.x -= y.x;
+            rhs.y -= y.y;
+        }
+        const double dd = 1.0 / (a[P].x * a[P].x + a[P].y * a[P].y);
+        U(k, 0) = make_double2(a[P].x * dd, -a[P].y * dd);
+#pragma unroll
+        for (int q = 1; q <= P; ++q) U(k, q) = a[P + q];
+        xl[(size_t)k * ks] = rhs;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        double2 v = xl[(size_t)k * ks];
+#pragma unroll
+        for (int q = 1; q <= P; ++q)
+            if (k + q < n) {
+                const double2 u = cm(U(k, q), xl[(size_t)(k + q) * ks]);
+                v.x -= u.x;
+                v.y -= u.y;
+            }
+        xl[(size_t)k * ks] = cm(v, U(k, 0));
+    }
+}
+
+void line_solve64(const PcFDM &f, double2 *x, cudaStream_t st) {
+    const int dim = f.dim, outer = dim - 1;
+    Line64Params lp{};
+    lp.x = x;
+    lp.n0 = f.n[0];
+    lp.n1 = dim == 3 ? f.n[1] : 1;
+    lp.n2 = f.n[outer];
+    lp.ks = (size_t)lp.n0 * lp.n1;
+    lp.js = lp.n0;
+    lp.bands = f.op->dev64[outer].as<double>();
+    lp.lx = f.lam[0].as<double>();
+    lp.ly = dim == 3 ? f.lam[1].as<double>() : nullptr;
+    if (f.cplx) {
+        lp.lxi = f.lami[0].as<double>();
+        lp.lyi = dim == 3 ? f.lami[1].as<double>() : nullptr;
+    }
+    line_combs<double>(f, lp.Bc, lp.Cc);
+    lp.U = f.ufac.as<double2>();
+    const int nl = lp.n0 * lp.n1, blocks = (nl + 127) / 128;
+    switch (f.P) {
+    case 2: k_line64<2><<<blocks, 128, 0, st>>>(lp); break;
+    case 3: k_line64<3><<<blocks, 128, 0, st>>>(lp); break;
+    case 4: k_line64<4><<<blocks, 128, 0, st>>>(lp); break;
+    case 5: k_line64<5><<<blocks, 128, 0, st>>>(lp); break;
+    }
+    TDZ_CUDA(cudaGetLastError());
+    count_launch();
 }
 
 void line_solve(int P, const ZSolveParams &zp, cudaStream_t st) {
@@ -1075,20 +1209,51 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
         ++applies;
         return;
     }
+    const int grows = (int)rows;
+    if (f64) {
+        // FP64 preconditioner (SIMT transforms, FP64 line solves)
+        double2 *y1 = b1.as<double2>(), *y2 = b2.as<double2>();
+        auto x64 = [&](const DevBuf &Mx, const double2 *in, double2 *out) {
+            const dim3 g((n[0] + BN - 1) / BN, (grows + BM - 1) / BM);
+            if (cplx) k_gemm_cr<double2, double2><<<g, 256, 0, st>>>(in, Mx.as<double2>(), out, grows, n[0], n[0]);
+            else k_gemm_cr<double2, double><<<g, 256, 0, st>>>(in, Mx.as<double>(), out, grows, n[0], n[0]);
+        };
+        auto y64 = [&](const DevBuf &My, const double2 *in, double2 *out) {
+            const dim3 g((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]);
+            if (cplx) k_gemm_rc<double2, double2><<<g, 256, 0, st>>>(My.as<double2>(), in, out, n[1], n[0], n[1]);
+            else k_gemm_rc<double2, double><<<g, 256, 0, st>>>(My.as<double>(), in, out, n[1], n[0], n[1]);
+        };
+        x64(V[0], r, y2);
+        double2 *cur = y2, *oth = y1;
+        if (dim == 3) {
+            y64(VT[1], y2, y1);
+            std::swap(cur, oth);
+        }
+        TDZ_CUDA(cudaGetLastError());
+        line_solve64(*this, cur, st);
+        if (dim == 3) {
+            y64(V[1], cur, oth);
+            std::swap(cur, oth);
+        }
+        x64(VT[0], cur, z);
+        TDZ_CUDA(cudaGetLastError());
+        count_launch(dim == 3 ? 4 : 2);
+        ++applies;
+        return;
+    }
     float2 *x1 = b1.as<float2>(), *x2 = b2.as<float2>();
     blas::cast(r, TDZ_FP64, x1, TDZ_FP32, N, st);
-    const int grows = (int)rows;
     // transforms along x (rows of n0) and along y (planes of n1 x n0) with a
     // real or complex FP32 matrix
     auto along_x = [&](const DevBuf &Mx, const float2 *in, float2 *out) {
         const dim3 g((n[0] + BN - 1) / BN, (grows + BM - 1) / BM);
-        if (cplx) k_gemm_cr<float2><<<g, 256, 0, st>>>(in, Mx.as<float2>(), out, grows, n[0], n[0]);
-        else k_gemm_cr<float><<<g, 256, 0, st>>>(in, Mx.as<float>(), out, grows, n[0], n[0]);
+        if (cplx) k_gemm_cr<float2, float2><<<g, 256, 0, st>>>(in, Mx.as<float2>(), out, grows, n[0], n[0]);
+        else k_gemm_cr<float2, float><<<g, 256, 0, st>>>(in, Mx.as<float>(), out, grows, n[0], n[0]);
     };
     auto along_y = [&](const DevBuf &My, const float2 *in, float2 *out) {
         const dim3 g((n[0] + BN - 1) / BN, (n[1] + BM - 1) / BM, n[2]);
-        if (cplx) k_gemm_rc<float2><<<g, 256, 0, st>>>(My.as<float2>(), in, out, n[1], n[0], n[1]);
-        else k_gemm_rc<float><<<g, 256, 0, st>>>(My.as<float>(), in, out, n[1], n[0], n[1]);
+        if (cplx) k_gemm_rc<float2, float2><<<g, 256, 0, st>>>(My.as<float2>(), in, out, n[1], n[0], n[1]);
+        else k_gemm_rc<float2, float><<<g, 256, 0, st>>>(My.as<float>(), in, out, n[1], n[0], n[1]);
     };
     // forward transforms: along x with V (t_i = sum_i' V[i'][i] r_i'), along y with V^T
     along_x(V[0], x1, x2);

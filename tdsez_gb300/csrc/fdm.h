@@ -21,7 +21,7 @@ bool gen_eig_complex(const std::vector<cd> &S, int p, const BandD &M, std::vecto
 // combinations of the outer-axis base bands. Then
 //   A^-1 = (V_x (x) V_y (x) I) [ (Bz + (lam_i + lam_j) Cz)^-1 ]_{ij} (V_x^T (x) V_y^T (x) I),
 // applied as dense transforms along x and y and one banded complex LU solve
-// per (i, j) line along z, in FP32.
+// per (i, j) line along z, in FP32 (tensor-core transforms in 3D) or FP64.
 struct PcFDM : Precond {
     Operator *op = nullptr;
     int dim = 0, P = 0;
@@ -56,7 +56,8 @@ struct PcFDM : Precond {
     // complex-shifted poles of the t-SURFF end term)
     bool pole = false;
     std::array<cd, 5> pole_sigma{};
-    void setup(Operator *op_);
+    bool f64 = false;          // FP64 preconditioner: SIMT FP64 transforms and FP64 line solves
+    void setup(Operator *op_, int prec = TDZ_FP32);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;
 };
 

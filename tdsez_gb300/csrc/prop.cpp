@@ -61,7 +61,7 @@ void Solver::setup(Operator *op_, const SolverOptions &o, cudaStream_t st) {
         pc = std::move(p);
     } else if (o.pc == 3) {
         auto p = std::make_unique<PcFDM>();
-        p->setup(op);
+        p->setup(op, o.pc_precision);
         pc = std::move(p);
     } else if (o.pc == 4) {
         auto p = std::make_unique<PcBand>();

@@ -31,6 +31,7 @@ struct EndTermStats {
     int max_its = 0;          // largest per node
     double dp_max = 0.0;      // largest node spacing
     double eta = 0.0;         // pole damping used
+    int damped = 0;           // nodes finished with the damped pole after a stagnating undamped start
     double seconds = 0.0;
 };
 

@@ -19,7 +19,9 @@
 // symmetric axis pencils). When that inverse is not exact (a non-separable
 // potential), it is built for the damped pole E (1 + i eta) (the
 // shifted-Laplacian rule the reference uses for its 3D poles) while FGMRES
-// solves the undamped system.
+// solves the undamped system; so is a node at which the exact FP32 inverse
+// stagnates (a weakly absorbed box mode next to E: the FP32 inverse of a
+// nearly singular stage has no correct digits left).
 // The flux of a node is added to the momenta that use it as soon as it is
 // solved, so no node solution is kept.
 #include <algorithm>
@@ -158,33 +160,53 @@ EndTermStats TSurff::end_term(Operator &op, const SolverOptions &so_in, const En
     sol.setup(&op, so, st);
     auto *fdm = so.pc == TDZ_PC_FDM ? static_cast<PcFDM *>(sol.pc.get()) : nullptr;
     auto *band = so.pc == TDZ_PC_BAND ? static_cast<PcBand *>(sol.pc.get()) : nullptr;
-    double eta = eo.eta;
-    if (eta < 0.0) eta = (fdm && !fdm->exact_now()) || (band && !band->exact) ? 0.5 : 0.0;
+    // pole damping: none for an exact inverse, 0.5 otherwise; with an exact
+    // FP32 inverse a node whose stage is nearly singular (a weakly absorbed
+    // box mode close to E) makes FGMRES stagnate, and that node is finished
+    // with the damped pole instead
+    const bool eta_auto = eo.eta < 0.0;
+    const bool exact_pc = (fdm && fdm->exact_now()) || (band && band->exact);
+    const double eta_base = eta_auto ? (exact_pc ? 0.0 : 0.5) : eo.eta;
+    const int maxit = so.maxit, first_its = 60;
 
     EndTermStats stats;
     stats.nodes = nn;
-    stats.eta = eta;
+    stats.eta = eta_base;
     for (int j = 0; j + 1 < nn; ++j) stats.dp_max = std::max(stats.dp_max, node[j + 1] - node[j]);
     for (int j = 0; j < nn; ++j) {
         const double E = energy(j);
-        const cd pole(E, eta * std::max(E, 1e-3));
-        if (band) {
-            // factor the pole, then solve the undamped system with it
-            op.set_stage(pole, cd(-1.0, 0.0), no_field);
-            band->factor(st);
+        auto prepare = [&](double eta) {
+            const cd pole(E, eta * std::max(E, 1e-3));
+            if (band) {
+                // factor the pole, then solve the undamped system with it
+                op.set_stage(pole, cd(-1.0, 0.0), no_field);
+                band->factor(st);
+            }
+            op.set_stage(cd(E, 0.0), cd(-1.0, 0.0), no_field);
+            if (fdm) {
+                fdm->pole = eta > 0.0;
+                fdm->pole_sigma = op.sigma;
+                fdm->pole_sigma[0] = pole;
+            }
+        };
+        const bool retry = eta_auto && eta_base == 0.0;
+        prepare(eta_base);
+        sol.opt.maxit = retry ? std::min(first_its, maxit) : maxit;
+        SolveStats ss = sol.solve(b.as<double2>(), x.as<double2>(), st);
+        int its = ss.its;
+        if (ss.reason <= 0 && retry) {
+            if (ss.reason == -9) blas::zero(x.ptr, N, TDZ_FP64, st);
+            prepare(0.5);
+            sol.opt.maxit = std::max(1, maxit - its);
+            ss = sol.solve(b.as<double2>(), x.as<double2>(), st);
+            its += ss.its;
+            ++stats.damped;
         }
-        op.set_stage(cd(E, 0.0), cd(-1.0, 0.0), no_field);
-        if (fdm) {
-            fdm->pole = eta > 0.0;
-            fdm->pole_sigma = op.sigma;
-            fdm->pole_sigma[0] = pole;
-        }
-        const SolveStats ss = sol.solve(b.as<double2>(), x.as<double2>(), st);
         TDZ_CHECK(ss.reason > 0, TDZ_ERR_NOT_CONVERGED,
                   "t-SURFF end term: the solve at E = " + std::to_string(E) + " did not converge (reason " +
-                      std::to_string(ss.reason) + ", " + std::to_string(ss.its) + " iterations)");
-        stats.its += ss.its;
-        stats.max_its = std::max(stats.max_its, ss.its);
+                      std::to_string(ss.reason) + ", " + std::to_string(its) + " iterations)");
+        stats.its += its;
+        stats.max_its = std::max(stats.max_its, its);
         add_weighted_flux(x.as<double2>(), eq.as<int>() + start[j], ew.as<double>() + start[j],
                           start[j + 1] - start[j], st);
     }

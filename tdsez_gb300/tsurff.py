@@ -74,7 +74,7 @@ class TSurff:
         o = _lib.tdz_tsurff_end_opts()
         o.dp, o.cap_width, o.eta, o.rtol, o.maxit = dp, cap_width, eta, rtol, maxit
         out = np.zeros(2 * int(np.prod(self.nk)))
-        st = np.zeros(6)
+        st = np.zeros(7)
         inner_p = C.cast(C.byref(inner), C.c_void_p) if inner is not None else None
         import torch
         s = torch.cuda.current_stream().cuda_stream if stream is None else stream
@@ -82,7 +82,7 @@ class TSurff:
                                                    C.c_void_p(psi.data_ptr()), _lib.dptr(out), _lib.dptr(st),
                                                    C.c_void_p(s)))
         stats = {"nodes": int(st[0]), "its": int(st[1]), "max_its": int(st[2]), "dp_max": float(st[3]),
-                 "eta": float(st[4]), "seconds": float(st[5])}
+                 "eta": float(st[4]), "seconds": float(st[5]), "damped": int(st[6])}
         return out.view(np.complex128), stats
 
     def volkov(self):

@@ -105,9 +105,9 @@ def test_end_term_parity(cuda, name, R, kg, dp):
     out, stats = gpu.end_term(op, torch.tensor(st, device=cuda), cap_width=width, dp=dp, rtol=1e-11)
     print(f"{name}: {stats}")
     assert stats["nodes"] == len(nodes)
-    # exact preconditioners: the banded LU (1D) and the FDM inverse with
-    # complex symmetric axis pencils (2D), so a few iterations per node
-    assert stats["eta"] == 0.0 and stats["max_its"] <= 6, stats
+    # exact preconditioners: the banded LU (1D) and the FP64 FDM inverse
+    # with complex symmetric axis pencils (2D), so one or two iterations per node
+    assert stats["eta"] == 0.0 and stats["max_its"] <= 3, stats
     err = np.abs(out - ref).max() / np.abs(ref).max()
     assert err < 1e-8, err
     # the flux part is unchanged by the end term
@@ -169,9 +169,8 @@ def test_end_term_end2d_on_the_gpu(cuda):
     w, k0 = 1.0, (2.0, 1.0)
     psi = op.separable_state([lambda x, k=k: (2 * np.pi * w * w) ** -0.25 * np.exp(-x * x / (4 * w * w) + 1j * k * x)
                               for k in k0])
-    fld = lambda t: [0.0, 0.0]
-    G = Propagator(op, "cn", field=fld, pc="fdm", precision="fp32", rtol=1e-12, guess_order=-1)
-    ts = TSurff(PS, 6.0, [(-1.0, 5.0, 31), (-2.0, 4.0, 31)], fld, 0.02)
+    G = Propagator(op, "cn", field=lambda t: [0.0], pc="fdm", precision="fp32", rtol=1e-12, guess_order=-1)
+    ts = TSurff(PS, 6.0, [(-1.0, 5.0, 31), (-2.0, 4.0, 31)], lambda t: [0.0, 0.0], 0.02)
     G.evolve(psi, 0.02, 2.0, monitor=lambda step, t, ps: ts.sample(t, ps))
     end, stats = ts.end_term(op, psi, cap_width=cap_width(1.0))
     print(stats)
@@ -181,7 +180,7 @@ def test_end_term_end2d_on_the_gpu(cuda):
                   (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ky - k0[1]) ** 2))
     err = np.abs(np.abs(b) ** 2 - ex).max() / ex.max()
     assert err < 1e-2, err
-    assert stats["max_its"] <= 8, stats
+    assert stats["max_its"] <= 3 and stats["damped"] == 0, stats
 
 
 @pytest.mark.gpu
