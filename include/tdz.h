@@ -465,7 +465,7 @@ typedef struct tdz_tsurff_end_opts {
     double cap_width;   /* absorbing-layer width; needed when dp = 0          */
     double eta;         /* preconditioner pole damping; < 0 = automatic      */
     double rtol;        /* per-node relative residual; 0 = 1e-10              */
-    int maxit;          /* per-node FGMRES iterations; 0 = 4000               */
+    int maxit;          /* per-node FGMRES iterations; 0 = 600                */
 } tdz_tsurff_end_opts;
 tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts *inner,
                                const tdz_tsurff_end_opts *o, const void *psi, double *out, double *stats,

@@ -9,10 +9,13 @@
 // For distinct eigenvalues the eigenvectors of a complex symmetric matrix
 // are orthogonal in the bilinear form x^T y; scaled to x^T x = 1 they give
 // Q^T C Q = diag(lam), Q^T Q = I, and V = L^-T Q satisfies V^T M V = I,
-// V^T S V = diag(lam). Both identities are checked before the result is
+// V^T S V = diag(lam). Clusters of equal eigenvalues (the mirror-image
+// modes of two absorbing layers) get an orthonormal basis of their invariant
+// subspace in that form. Both identities are checked before the result is
 // used.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 
 #include "fdm.h"
 
@@ -171,7 +174,7 @@ bool gen_eig_complex(const std::vector<cd> &S, int p, const BandD &M, std::vecto
     to_hessenberg(C, Z, n);
     schur(C, Z, n);
 
-    // eigenvectors of T by back-substitution, then Q = Z Y, scaled to q^T q = 1
+    // eigenvectors of T by back-substitution, then Q = Z Y
     lam.resize(n);
     for (int k = 0; k < n; ++k) lam[k] = C[(size_t)k * n + k];
     const double small = 1e-14 * std::max(cnorm, 1e-300);
@@ -187,16 +190,139 @@ bool gen_eig_complex(const std::vector<cd> &S, int p, const BandD &M, std::vecto
             if (std::abs(den) < small) den = small;
             y[i] = -sum / den;
         }
-        cd qq = 0.0;
+        double nrm = 0.0;
         for (int i = 0; i < n; ++i) {
             cd v = 0.0;
             for (int j = 0; j <= k; ++j) v += Z[(size_t)i * n + j] * y[j];
             Q[(size_t)i * n + k] = v;
-            qq += v * v;
+            nrm += std::norm(v);
         }
-        if (std::abs(qq) < 1e-300) return false;   // self-orthogonal vector: no bilinear scaling
-        const cd sc = 1.0 / std::sqrt(qq);
-        for (int i = 0; i < n; ++i) Q[(size_t)i * n + k] *= sc;
+        nrm = 1.0 / std::sqrt(nrm);
+        for (int i = 0; i < n; ++i) Q[(size_t)i * n + k] *= nrm;
+    }
+    auto col_dot = [&](int a, int b) {   // bilinear q_a^T q_b
+        cd g = 0.0;
+        for (int i = 0; i < n; ++i) g += Q[(size_t)i * n + a] * Q[(size_t)i * n + b];
+        return g;
+    };
+    // Clusters of (nearly) equal eigenvalues: mirror-image modes of the two
+    // absorbing layers come in pairs whose splitting is at rounding level, so
+    // the computed vectors of a pair are arbitrary mixtures. Each cluster
+    // gets a bilinear-orthonormal basis of its invariant subspace (pivoted
+    // Gram-Schmidt in the form x^T y), and the cluster block Q_c^T C Q_c is
+    // diagonalised by complex symmetric Jacobi rotations.
+    std::vector<int> cl(n);
+    for (int k = 0; k < n; ++k) cl[k] = k;
+    std::function<int(int)> root = [&](int k) { return cl[k] == k ? k : cl[k] = root(cl[k]); };
+    for (int a = 0; a < n; ++a)
+        for (int b = a + 1; b < n; ++b)
+            if (std::abs(lam[a] - lam[b]) <= 1e-6 * std::max({std::abs(lam[a]), std::abs(lam[b]), 1e-300}))
+                cl[root(a)] = root(b);
+    double coupling = 0.0;   // largest off-diagonal entry left in a cluster block
+    std::vector<std::vector<int>> groups(n);
+    for (int k = 0; k < n; ++k) groups[root(k)].push_back(k);
+    for (const std::vector<int> &g : groups) {
+        if (g.empty()) continue;
+        const int m = (int)g.size();
+        // pivoted bilinear Gram-Schmidt
+        std::vector<int> left = g, done;
+        while (!left.empty()) {
+            int best = -1;
+            double bq = -1.0;
+            for (int k : left) {
+                double nn = 0.0;
+                for (int i = 0; i < n; ++i) nn += std::norm(Q[(size_t)i * n + k]);
+                const double r = std::abs(col_dot(k, k)) / std::max(nn, 1e-300);
+                if (r > bq) { bq = r; best = k; }
+            }
+            if (!(bq > 1e-6)) return false;   // isotropic subspace: no bilinear-orthonormal basis
+            const cd sc = 1.0 / std::sqrt(col_dot(best, best));
+            for (int i = 0; i < n; ++i) Q[(size_t)i * n + best] *= sc;
+            left.erase(std::find(left.begin(), left.end(), best));
+            for (int k : left) {
+                const cd h = col_dot(best, k);
+                for (int i = 0; i < n; ++i) Q[(size_t)i * n + k] -= h * Q[(size_t)i * n + best];
+            }
+            done.push_back(best);
+        }
+        if (m == 1) continue;
+        // G = Q_c^T C0 Q_c, diagonalised by rotations R = [c s; -s c], c^2 + s^2 = 1
+        Mat G((size_t)m * m), CQ((size_t)n * m);
+        for (int b = 0; b < m; ++b)
+            for (int i = 0; i < n; ++i) {
+                cd v = 0.0;
+                for (int j = 0; j < n; ++j) v += C0[(size_t)i * n + j] * Q[(size_t)j * n + g[b]];
+                CQ[(size_t)i * m + b] = v;
+            }
+        for (int a = 0; a < m; ++a)
+            for (int b = 0; b < m; ++b) {
+                cd v = 0.0;
+                for (int i = 0; i < n; ++i) v += Q[(size_t)i * n + g[a]] * CQ[(size_t)i * m + b];
+                G[(size_t)a * m + b] = v;
+            }
+        for (int a = 0; a < m; ++a)
+            for (int b = 0; b < a; ++b) G[(size_t)a * m + b] = G[(size_t)b * m + a] = 0.5 * (G[(size_t)a * m + b] + G[(size_t)b * m + a]);
+        // near an exceptional point (coalescing eigenvectors) the rotations
+        // blow up: the cluster then keeps its orthonormal basis and the
+        // diagonal of G, and the off-diagonal coupling (at most the
+        // cluster's eigenvalue spread) is left to the Krylov method
+        const Mat G0 = G;
+        Mat Qsave((size_t)n * m);
+        for (int b = 0; b < m; ++b)
+            for (int i = 0; i < n; ++i) Qsave[(size_t)i * m + b] = Q[(size_t)i * n + g[b]];
+        bool ep = false;
+        for (int sweep = 0; sweep < 30 && !ep; ++sweep) {
+            double off = 0.0, tot = 0.0;
+            for (int a = 0; a < m; ++a)
+                for (int b = 0; b < m; ++b) {
+                    tot += std::norm(G[(size_t)a * m + b]);
+                    if (a != b) off += std::norm(G[(size_t)a * m + b]);
+                }
+            if (off <= 1e-28 * tot) break;
+            for (int pa = 0; pa < m - 1 && !ep; ++pa) {
+                for (int qa = pa + 1; qa < m; ++qa) {
+                    const cd gpq = G[(size_t)pa * m + qa];
+                    // rounding-level coupling of (numerically) equal eigenvalues: nothing to rotate
+                    if (std::abs(gpq) <= 1e-14 * (std::abs(G[(size_t)pa * m + pa]) + std::abs(G[(size_t)qa * m + qa])))
+                        continue;
+                    const cd dg = G[(size_t)pa * m + pa] - G[(size_t)qa * m + qa];
+                    const cd root2 = std::sqrt(dg * dg + 4.0 * gpq * gpq);
+                    const cd den = std::abs(dg + root2) >= std::abs(dg - root2) ? dg + root2 : dg - root2;
+                    const cd t = std::abs(den) > 0.0 ? 2.0 * gpq / den : cd(0.0);   // smaller root of gpq t^2 - dg t - gpq
+                    const cd w = 1.0 + t * t;
+                    if (!(std::abs(den) > 0.0) || std::abs(w) < 1e-3 || std::abs(t) > 1e3) {
+                        ep = true;
+                        break;
+                    }
+                    const cd c = 1.0 / std::sqrt(w), sn = t * c;
+                    // G <- R^T G R, Q_c <- Q_c R
+                    for (int k = 0; k < m; ++k) {
+                        const cd gkp = G[(size_t)k * m + pa], gkq = G[(size_t)k * m + qa];
+                        G[(size_t)k * m + pa] = c * gkp - sn * gkq;
+                        G[(size_t)k * m + qa] = sn * gkp + c * gkq;
+                    }
+                    for (int k = 0; k < m; ++k) {
+                        const cd gpk = G[(size_t)pa * m + k], gqk = G[(size_t)qa * m + k];
+                        G[(size_t)pa * m + k] = c * gpk - sn * gqk;
+                        G[(size_t)qa * m + k] = sn * gpk + c * gqk;
+                    }
+                    for (int i = 0; i < n; ++i) {
+                        const cd qp = Q[(size_t)i * n + g[pa]], qq = Q[(size_t)i * n + g[qa]];
+                        Q[(size_t)i * n + g[pa]] = c * qp - sn * qq;
+                        Q[(size_t)i * n + g[qa]] = sn * qp + c * qq;
+                    }
+                }
+            }
+        }
+        if (ep) {
+            G = G0;
+            for (int b = 0; b < m; ++b)
+                for (int i = 0; i < n; ++i) Q[(size_t)i * n + g[b]] = Qsave[(size_t)i * m + b];
+            for (int a = 0; a < m; ++a)
+                for (int b = 0; b < m; ++b)
+                    if (a != b) coupling = std::max(coupling, std::abs(G[(size_t)a * m + b]));
+        }
+        for (int a = 0; a < m; ++a) lam[g[a]] = G[(size_t)a * m + a];
     }
     // checks: Q^T Q = I and C Q = Q diag(lam)
     double orth = 0.0, res = 0.0;
@@ -210,7 +336,9 @@ bool gen_eig_complex(const std::vector<cd> &S, int p, const BandD &M, std::vecto
             orth = std::max(orth, std::abs(g - (a == b ? cd(1.0) : cd(0.0))));
             res = std::max(res, std::abs(r - Q[(size_t)a * n + b] * lam[b]));
         }
-    if (!(orth <= 1e-8) || !(res <= 1e-10 * std::max(cnorm, 1e-300) * std::sqrt((double)n))) return false;
+    if (!(coupling <= 1e-6 * std::max(cnorm, 1e-300))) return false;
+    if (!(orth <= 1e-6) || !(res <= 1e-10 * std::max(cnorm, 1e-300) * std::sqrt((double)n) + 2.0 * coupling))
+        return false;
     // V = L^-T Q (back-substitution with L^T, column by column)
     V.assign((size_t)n * n, cd(0.0));
     for (int c = 0; c < n; ++c)

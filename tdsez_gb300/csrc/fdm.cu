@@ -981,7 +981,8 @@ void PcFDM::setup(Operator *op_, int prec) {
         }
     }
     if (f64) {
-        ufac.alloc(N * (P + 1) * sizeof(double2));
+        ufac.alloc(N * (3 * P + 1) * sizeof(double2));
+        piv64.alloc(N * sizeof(int));
         b1.alloc(N * sizeof(double2));
         b2.alloc(N * sizeof(double2));
         return;
@@ -1073,8 +1074,9 @@ ZSolveParams line_params(const PcFDM &f) {
 }
 
 // FP64 line solves (the FP64 preconditioner): one thread per line, banded LU
-// without pivoting as in the FP32 solves, the U rows kept in a global
-// scratch, the line matrices evaluated from the FP64 bands row by row
+// with partial pivoting (the lines of the end term's indefinite stages need
+// it), the line matrix evaluated from the FP64 bands into a global scratch
+// whose row r holds columns r - P .. r + 2P, lines interleaved (coalesced)
 struct Line64Params {
     double2 *x;               // line (i, j), row k at x[k ks + j js + i]
     size_t ks;
@@ -1083,11 +1085,12 @@ struct Line64Params {
     const double *bands;      // outer base bands [nb][n2][2P+1] (FP64)
     const double *lx, *ly, *lxi, *lyi;
     CombP<double> Bc, Cc;
-    double2 *U;               // [n2][P + 1][lines]: reciprocal pivot, then the upper band
+    double2 *U;               // [n2][3P + 1][lines]: the line's LU factors
+    int *piv;                 // [n2][lines]: row interchanged with row k at step k
 };
 
 template <int P> __global__ void __launch_bounds__(128) k_line64(const Line64Params prm) {
-    constexpr int BW = 2 * P + 1;
+    constexpr int BW = 2 * P + 1, W = 3 * P + 1;
     const int nl = prm.n0 * prm.n1;
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nl) return;
@@ -1097,49 +1100,73 @@ template <int P> __global__ void __launch_bounds__(128) k_line64(const Line64Par
     double2 *xl = prm.x + (size_t)j * prm.js + i;
     const int n = prm.n2;
     const size_t ks = prm.ks;
-    auto U = [&](int k, int q) -> double2 & { return prm.U[((size_t)k * (P + 1) + q) * nl + l]; };
+    // entry (r, c) of the line matrix, |c - r| within the widened band
+    auto A = [&](int r, int c) -> double2 & { return prm.U[((size_t)r * W + (c - r + P)) * nl + l]; };
     auto cm = [](double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
-    for (int k = 0; k < n; ++k) {
-        double2 a[BW];
-#pragma unroll
-        for (int o = 0; o < BW; ++o) {
-            const double2 b = comb_at<double, double2>(prm.Bc, prm.bands, n, BW, k, o);
-            const double2 c = comb_at<double, double2>(prm.Cc, prm.bands, n, BW, k, o);
-            a[o] = make_double2(b.x + sr * c.x - si * c.y, b.y + sr * c.y + si * c.x);
-        }
-        double2 rhs = xl[(size_t)k * ks];
-#pragma unroll
-        for (int d = P; d >= 1; --d) {
-            const int r = k - d;
-            if (r < 0) continue;
-            const double2 f = cm(a[P - d], U(r, 0));
-#pragma unroll
-            for (int q = 1; q <= P; ++q) {
-                if (P - d + q >= BW) break;
-                const double2 u = cm(f, U(r, q));
-                a[P - d + q].x -= u.x;
-                a[P - d + q].y -= u.y;
+    for (int r = 0; r < n; ++r)
+        for (int o = 0; o < W; ++o) {
+            double2 v = make_double2(0.0, 0.0);
+            if (o < BW) {
+                const double2 b = comb_at<double, double2>(prm.Bc, prm.bands, n, BW, r, o);
+                const double2 c = comb_at<double, double2>(prm.Cc, prm.bands, n, BW, r, o);
+                v = make_double2(b.x + sr * c.x - si * c.y, b.y + sr * c.y + si * c.x);
             }
-            const double2 y = cm(f, xl[(size_t)r * ks]);
-            rhs.x -= y.x;
-            rhs.y -= y.y;
+            prm.U[((size_t)r * W + o) * nl + l] = v;
         }
-        const double dd = 1.0 / (a[P].x * a[P].x + a[P].y * a[P].y);
-        U(k, 0) = make_double2(a[P].x * dd, -a[P].y * dd);
-#pragma unroll
-        for (int q = 1; q <= P; ++q) U(k, q) = a[P + q];
-        xl[(size_t)k * ks] = rhs;
+    for (int k = 0; k < n; ++k) {
+        const int rmax = min(k + P, n - 1), cmax = min(k + 2 * P, n - 1);
+        int bi = k;
+        double best = fabs(A(k, k).x) + fabs(A(k, k).y);
+        for (int r = k + 1; r <= rmax; ++r) {
+            const double m = fabs(A(r, k).x) + fabs(A(r, k).y);
+            if (m > best) { best = m; bi = r; }
+        }
+        prm.piv[(size_t)k * nl + l] = bi;
+        if (!(best > 0.0)) continue;   // singular column: the solve returns non-finite values
+        if (bi != k)
+            for (int c = k; c <= cmax; ++c) {
+                const double2 t = A(k, c);
+                A(k, c) = A(bi, c);
+                A(bi, c) = t;
+            }
+        const double2 d = A(k, k);
+        const double dd = 1.0 / (d.x * d.x + d.y * d.y);
+        const double2 inv = make_double2(d.x * dd, -d.y * dd);
+        for (int r = k + 1; r <= rmax; ++r) {
+            const double2 f = cm(A(r, k), inv);
+            A(r, k) = f;
+            for (int c = k + 1; c <= cmax; ++c) {
+                const double2 u = cm(f, A(k, c));
+                double2 &t = A(r, c);
+                t.x -= u.x;
+                t.y -= u.y;
+            }
+        }
+    }
+    for (int k = 0; k < n; ++k) {
+        const int q = prm.piv[(size_t)k * nl + l];
+        if (q != k) {
+            const double2 t = xl[(size_t)k * ks];
+            xl[(size_t)k * ks] = xl[(size_t)q * ks];
+            xl[(size_t)q * ks] = t;
+        }
+        const double2 xk = xl[(size_t)k * ks];
+        for (int r = k + 1; r <= min(k + P, n - 1); ++r) {
+            const double2 u = cm(A(r, k), xk);
+            xl[(size_t)r * ks].x -= u.x;
+            xl[(size_t)r * ks].y -= u.y;
+        }
     }
     for (int k = n - 1; k >= 0; --k) {
         double2 v = xl[(size_t)k * ks];
-#pragma unroll
-        for (int q = 1; q <= P; ++q)
-            if (k + q < n) {
-                const double2 u = cm(U(k, q), xl[(size_t)(k + q) * ks]);
-                v.x -= u.x;
-                v.y -= u.y;
-            }
-        xl[(size_t)k * ks] = cm(v, U(k, 0));
+        for (int c = k + 1; c <= min(k + 2 * P, n - 1); ++c) {
+            const double2 u = cm(A(k, c), xl[(size_t)c * ks]);
+            v.x -= u.x;
+            v.y -= u.y;
+        }
+        const double2 d = A(k, k);
+        const double dd = 1.0 / (d.x * d.x + d.y * d.y);
+        xl[(size_t)k * ks] = make_double2((v.x * d.x + v.y * d.y) * dd, (v.y * d.x - v.x * d.y) * dd);
     }
 }
 
@@ -1161,6 +1188,7 @@ void line_solve64(const PcFDM &f, double2 *x, cudaStream_t st) {
     }
     line_combs<double>(f, lp.Bc, lp.Cc);
     lp.U = f.ufac.as<double2>();
+    lp.piv = f.piv64.as<int>();
     const int nl = lp.n0 * lp.n1, blocks = (nl + 127) / 128;
     switch (f.P) {
     case 2: k_line64<2><<<blocks, 128, 0, st>>>(lp); break;

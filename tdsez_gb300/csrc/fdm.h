@@ -57,6 +57,8 @@ struct PcFDM : Precond {
     bool pole = false;
     std::array<cd, 5> pole_sigma{};
     bool f64 = false;          // FP64 preconditioner: SIMT FP64 transforms and FP64 line solves
+                               // (partial pivoting; factors in ufac, interchanges in piv64)
+    DevBuf piv64;
     void setup(Operator *op_, int prec = TDZ_FP32);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;
 };

@@ -23,7 +23,7 @@ struct EndTermOptions {
     double cap_width = 0.0;   // width of the absorbing layer (sets the refined range below 2 k_cap)
     double eta = -1.0;        // pole damping of the preconditioner: E (1 + i eta); < 0 = automatic
     double rtol = 1e-10;      // relative residual of every node's solve
-    int maxit = 4000;         // FGMRES iterations per node
+    int maxit = 600;          // FGMRES iterations per node
 };
 struct EndTermStats {
     int nodes = 0;            // energy nodes

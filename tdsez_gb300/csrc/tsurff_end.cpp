@@ -155,7 +155,7 @@ EndTermStats TSurff::end_term(Operator &op, const SolverOptions &so_in, const En
     op.set_stage(cd(energy(0), 0.0), cd(-1.0, 0.0), no_field);
     SolverOptions so = so_in;
     so.rtol = eo.rtol > 0.0 ? eo.rtol : 1e-10;
-    so.maxit = eo.maxit > 0 ? eo.maxit : 4000;
+    so.maxit = eo.maxit > 0 ? eo.maxit : 600;
     Solver sol;
     sol.setup(&op, so, st);
     auto *fdm = so.pc == TDZ_PC_FDM ? static_cast<PcFDM *>(sol.pc.get()) : nullptr;
