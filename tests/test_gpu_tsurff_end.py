@@ -128,7 +128,7 @@ def test_end_term_end1d_on_the_gpu(cuda):
     from tdsez_gb300.space import Space
     from tdsez_gb300.tsurff import TSurff
     p, L = 7, 40.0
-    PS = Space([ob.uniform_knots(393, -L, L, p)], p, 10)
+    PS = Space([ob.uniform_knots(400, -L, L, p)], p, 10)
     op = Operator(PS, Physics(cap_kmin=0.5, bounds=[(-L, L)], coupled=(0,)))
     fld = lambda t: [0.2 * math.sin(math.pi * t / 15) ** 2 * math.sin(1.3 * t) if t < 15 else 0.0]
     w, k0 = 1.0, 0.8
@@ -152,7 +152,7 @@ def test_end_term_end1d_on_the_gpu(cuda):
 
 @pytest.mark.gpu
 def test_end_term_end2d_on_the_gpu(cuda):
-    """2D deck of the reference's end-term test (p = 4, 56 x 56 elements on
+    """2D deck of the reference's end-term test (p = 4, 60 x 60 elements on
     [-20, 20]^2, CAP k_min 1, CN dt 0.02 to T = 2, packet k0 = (2, 1), R = 6,
     31 x 31 momenta on [-1, 5] x [-2, 4], no field): the packet is still inside
     the box at T; flux plus end term give the analytic spectrum to 1e-2."""
@@ -163,7 +163,7 @@ def test_end_term_end2d_on_the_gpu(cuda):
     from tdsez_gb300.space import Space
     from tdsez_gb300.tsurff import TSurff
     p, L = 4, 20.0
-    kn = ob.uniform_knots(56, -L, L, p)
+    kn = ob.uniform_knots(60, -L, L, p)
     PS = Space([kn, kn], p, 6)
     op = Operator(PS, Physics(cap_kmin=1.0, bounds=[(-L, L), (-L, L)], coupled=(0,)))
     w, k0 = 1.0, (2.0, 1.0)

@@ -20,7 +20,7 @@ from oracle import propagate as opg
 from oracle import tsurff as ots
 
 
-def end1d_run(nel=393):
+def end1d_run(nel=400):
     """END1D: p = 7, [-40, 40], CAP k_min 0.5, Pade(2,2) dt 0.025, R = 10,
     181 momenta in [-1.5, 3], LaserX = 0.2 sin^2(pi t / 15) sin(1.3 t) for t < 15."""
     p, L = 7, 40.0
