@@ -9,7 +9,8 @@ stage solve (M + i dt/2 H_E) X = M psi to ||b - A X|| <= 1e-10 ||b|| in FP64
 Arms (same workload, same stopping rule):
   value      FP64 FGMRES with double-float applies, FP32 fast-diagonalisation
              preconditioner (--pc fdm, default), initial guess x0 = P^-1 b
-  mixed_mg   FP64 FGMRES, FP32 geometric B-spline multigrid
+  mixed_mg   FP64 FGMRES, FP32 geometric B-spline multigrid (mixed_mg_exact_coarse:
+             the same with the coarsest level solved by its exact FDM inverse)
   plain_mg   the plain GPU multigrid form: the same multigrid in FP64
 e2e: the same steps through the C ABI with the state in pinned host memory,
 copied host->device before and device->host after every step.
@@ -305,6 +306,12 @@ def run_tdz(args):
         return {"steps_per_s": nsteps / tpl, "its_per_step": (sp1["its"] - sp0["its"]) / nsteps, "steps": nsteps}
 
     mixed_mg = run_arm("fp32", args.mg_steps, outer=args.outer, **mg) if args.mg_steps > 0 else None
+    # the same multigrid with the coarsest level solved exactly by its FDM
+    # inverse (the role of the reference's coarse LU)
+    exact_coarse = None
+    if args.mg_steps > 0:
+        exact_coarse = run_arm("fp32", args.mg_steps, outer=args.outer, mg_coarse="fdm", **mg)
+        exact_coarse["what"] = "FP32 multigrid, coarsest level by the exact FDM inverse, in FP64 FGMRES"
 
     # ---- learned arm: FP32 multigrid with the learned coarse correction, its
     # network trained on the coarse right-hand sides of the run's own first
@@ -360,6 +367,7 @@ def run_tdz(args):
                           "tensor-core transforms (no BF16x3)",
         "vs_plain_mg": (value / plain["steps_per_s"]) if plain else None,
         "mixed_mg": mixed_mg,
+        "mixed_mg_exact_coarse": exact_coarse,
         "plain_mg": plain,
         "learned_mg": learned["learned"] if learned else None,
         "mixed_mg_same_levels": learned["plain"] if learned else None,

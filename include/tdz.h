@@ -219,6 +219,12 @@ typedef struct tdz_solver_opts {
                            whenever a stage solve takes more than this many
                            iterations (-tdsez_pc_refresh_its); 0 = only the
                            2 base + 5 rule of tdz_pc_refresh_stale           */
+    int mg_coarse;      /* coarsest-level solve of TDZ_PC_MG: 0 = Chebyshev
+                           polynomial of degree mg_coarse_its; 1 = the FDM
+                           inverse of the coarsest operator when it is exact
+                           there (separable stage; the role of the reference's
+                           coarse LU, src/multigrid.cpp:314-325), else the
+                           polynomial                                         */
 } tdz_solver_opts;
 /* Set up the solver for the current stage of op (call set_stage first). */
 tdz_status tdz_solver_create(tdz_op *op, const tdz_solver_opts *opts, void *stream, tdz_solver **out);

@@ -55,6 +55,7 @@ class tdz_solver_opts(C.Structure):
         ("mg_learned", C.c_int),
         ("relaxed", C.c_int),
         ("pc_refresh_its", C.c_int),
+        ("mg_coarse", C.c_int),
     ]
 
 

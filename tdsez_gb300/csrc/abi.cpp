@@ -273,6 +273,8 @@ static tdz::SolverOptions solver_options(const tdz_solver_opts *o) {
     so.mg.learned = o->mg_learned;
     so.relaxed = o->relaxed != 0;
     so.pc_refresh_its = o->pc_refresh_its > 0 ? o->pc_refresh_its : -1;
+    TDZ_CHECK(o->mg_coarse == 0 || o->mg_coarse == 1, TDZ_ERR_ARG, "mg_coarse must be 0 or 1");
+    so.mg.coarse_fdm = o->mg_coarse;
     TDZ_CHECK(so.outer == TDZ_FP64 || so.outer == TDZ_FP64_DF, TDZ_ERR_ARG,
               "outer_precision must be TDZ_FP64 or TDZ_FP64_DF");
     return so;

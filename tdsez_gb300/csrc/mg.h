@@ -16,6 +16,7 @@
 
 #include "blas.h"
 #include "cnn.h"
+#include "fdm.h"
 #include "krylov.h"
 #include "linesolve.h"
 #include "oper.h"
@@ -51,6 +52,8 @@ struct MGOptions {
     double ratio = 60.0;     // smoothing range [mu_hi / ratio, mu_hi]
     int precision = TDZ_FP32;
     int learned = 0;         // 1: CNN correction of the coarsest solve (FP32 levels)
+    int coarse_fdm = 0;      // 1: coarsest level solved by the FDM inverse where it is exact
+                             //    (the role of the reference's coarse LU), else the polynomial
 };
 
 // Learned coarse correction: after the Chebyshev coarse solve x0 of A_c x = b_c,
@@ -85,6 +88,9 @@ struct Multigrid : Precond {
     long long cycles = 0;
     blas::Reducer red;
     LearnedCoarse lrn;
+    std::unique_ptr<PcFDM> cfdm;          // exact coarsest-level inverse (coarse_fdm)
+    DevBuf cb64, cx64;                    // its FP64 right-hand side and solution
+    long long coarse_exact = 0;           // coarsest solves done by it
 
     void setup(Operator *fine_, const MGOptions &o, cudaStream_t st);
     void estimate_bounds(cudaStream_t st);

@@ -247,6 +247,17 @@ void Multigrid::setup(Operator *fine_, const MGOptions &o, cudaStream_t st) {
     red.init();
     estimate_bounds(st);
     if (opt.learned) learned_setup();
+    if (opt.coarse_fdm && !lrn.on) {
+        MGLevel &c = lv.back();
+        const int P = c.space.ax[0].p;
+        if (c.space.dim >= 2 && P >= 2 && P <= 5 && c.space.ax[1].p == P && (c.space.dim < 3 || c.space.ax[2].p == P)) {
+            c.opp->sigma = fine->sigma;
+            cfdm = std::make_unique<PcFDM>();
+            cfdm->setup(c.opp, prec);
+            cb64.alloc(c.ndof * sizeof(double2));
+            cx64.alloc(c.ndof * sizeof(double2));
+        }
+    }
 }
 
 namespace {
@@ -369,6 +380,14 @@ void Multigrid::vcycle(int l, cudaStream_t st) {
         if (lrn.on && lrn.rec_n < lrn.rec_cap) {   // a training input from this run
             blas::copy(m.b.ptr, lrn.rec.as<float2>() + (size_t)lrn.rec_n * m.ndof, m.ndof, TDZ_FP32, st);
             ++lrn.rec_n;
+        }
+        if (cfdm && !lrn.on && cfdm->exact_now()) {
+            // the exact fast-diagonalisation inverse of the coarsest operator
+            blas::cast(m.b.ptr, prec, cb64.ptr, TDZ_FP64, m.ndof, st);
+            cfdm->apply(cb64.as<double2>(), cx64.as<double2>(), st);
+            blas::cast(cx64.ptr, TDZ_FP64, m.x.ptr, prec, m.ndof, st);
+            ++coarse_exact;
+            return;
         }
         chebyshev(m, prec, m.mu_lo, m.mu_hi, m.w_max, opt.coarse_its, true, st);
         if (lrn.on && lrn.trained) coarse_correct(m, st);

@@ -27,13 +27,16 @@ MAGNUS_C = (0.5 - S3 / 6.0, 0.5 + S3 / 6.0)
 
 def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, restart: int = 0,
                 maxit: int = 1000, mg_levels: int = 0, mg_smooth: int = 0, mg_coarse_its: int = 12,
-                outer: str = "fp64", mg_learned: bool = False, relaxed: bool = False, pc_refresh_its: int = 0):
+                outer: str = "fp64", mg_learned: bool = False, relaxed: bool = False, pc_refresh_its: int = 0,
+                mg_coarse: str = "chebyshev"):
     """Solver options. ``precision`` is the preconditioner's arithmetic
     (fp32 = mixed precision); ``outer`` the arithmetic of the FP64 Krylov
     method's operator applies: "fp64" (native) or "df" (double-float on the
     FP32 pipes, about 48 significant bits). ``pc_refresh_its`` > 0 also
     rebuilds a propagator's preconditioner whenever a stage solve takes more
-    iterations (-tdsez_pc_refresh_its)."""
+    iterations (-tdsez_pc_refresh_its). ``mg_coarse``: "chebyshev" (the
+    polynomial of degree mg_coarse_its) or "fdm" (the exact FDM inverse of
+    the coarsest operator where the stage is separable)."""
     o = _lib.tdz_solver_opts()
     o.restart = restart
     o.maxit = maxit
@@ -47,6 +50,7 @@ def solver_opts(pc: str = "mg", precision: str = "fp32", rtol: float = 1e-12, re
     o.mg_learned = 1 if mg_learned else 0
     o.relaxed = 1 if relaxed else 0
     o.pc_refresh_its = max(0, int(pc_refresh_its))
+    o.mg_coarse = {"chebyshev": 0, "fdm": 1}[mg_coarse]
     return o
 
 

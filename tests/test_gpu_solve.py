@@ -89,6 +89,40 @@ def test_fdm_solve(cuda, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name,cc", [("3d_heterostructure", [0.02]), ("3d_const_mass_cap", [0.0, 0.02]),
+                                     ("2d_cap_free", [0.0])])
+def test_mg_exact_coarse_solve(cuda, name, cc):
+    """The coarsest multigrid level solved by the FDM inverse (mg_coarse =
+    "fdm", in the role of the reference's coarse LU): the same FP64
+    solution, in no more FGMRES iterations than with the Chebyshev coarse
+    polynomial; on the single-level CAP case the V-cycle becomes the exact
+    inverse."""
+    import torch
+    from tdsez_gb300.propagator import Solver
+    c = CASES[name]()
+    S, ph, A = oracle_of(c)
+    PS, op = product_of(c)
+    tau = 0.2
+    op.set_stage(1.0, 1j * tau, cc)
+    Am = (A.M + 1j * tau * (A.H_total() + sum(ck * T for ck, T in zip(cc, A.terms())))).tocsc()
+    rng = np.random.default_rng(11)
+    b = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
+    xref = sla.spsolve(Am, b)
+    bd = torch.tensor(b, device=cuda)
+    its = {}
+    for coarse in ("chebyshev", "fdm"):
+        s = Solver(op, pc="mg", precision="fp32", rtol=1e-12, maxit=400, mg_coarse=coarse)
+        xd = torch.zeros_like(bd)
+        its[coarse], reason, rn = s.solve(bd, xd)
+        assert reason > 0, (coarse, its, reason)
+        assert _rel(xd.cpu().numpy(), xref) < 1e-9
+    print(name, its)
+    assert its["fdm"] <= its["chebyshev"], its
+    if S.ndof < 2000:       # one level: the V-cycle is the exact inverse
+        assert its["fdm"] <= 4, its
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 @pytest.mark.parametrize("name,cc", [("2d_cap_free", [0.0]), ("2d_cap_softcore_sep", [0.0]),
                                      ("3d_const_mass_cap", [0.0, 0.03])])
