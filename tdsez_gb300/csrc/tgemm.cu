@@ -28,8 +28,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <set>
 
 namespace tdz {
@@ -53,6 +55,10 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
@@ -316,6 +322,183 @@ __global__ void __launch_bounds__(160, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
+// Warp-specialised variant with double-buffered accumulators (320 threads,
+// one CTA per SM, 128-row tiles):
+//   warps 0-3  split each A chunk into TF32 hi (in place) and lo (a buffer of
+//              the same stage), then arrive on the stage's `split` barrier;
+//   warp 9     (one thread) issues the stage's MMAs into accumulator
+//              tile & 1 (TMEM columns 0 or 256) and commits them to the
+//              stage's `done` barrier, and at the end of a tile to `accf`;
+//   warps 4-7  drain accumulator tile & 1 (warp w reads TMEM lanes
+//              32 (w % 4)..) into the transposed output, then arrive on
+//              `acce`, so the MMAs of the next tile run meanwhile;
+//   warp 8     (one thread) keeps the stage ring full with TMA.
+// The lo part lives in its stage, so the split of a chunk never waits for
+// MMAs (the producer recycles a stage only after its MMAs completed).
+template <int NP> struct WSShape {
+    static constexpr int B_BYTES = NP * KC * 4;
+    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;   // A (hi in place), A lo, B hi, B lo
+    static constexpr size_t smem_for(int ns) { return 1024 + (size_t)ns * STAGE + (3 * ns + 4) * 8 + 16; }
+    static constexpr int NS = smem_for(6) <= 232448   ? 6
+                              : smem_for(5) <= 232448 ? 5
+                              : smem_for(4) <= 232448 ? 4
+                              : smem_for(3) <= 232448 ? 3
+                                                      : 2;
+    static constexpr size_t SMEM = smem_for(NS);
+    static constexpr bool fits = SMEM <= 232448;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(320, 1)
+    k_transform_ws(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
+                   const TGParams prm) {
+    using S = WSShape<NP>;
+    constexpr int NS = S::NS, STAGE = S::STAGE, B_BYTES = S::B_BYTES;
+    constexpr uint32_t TMEM_COLS = 512;   // two accumulators, columns 0 and 256
+    static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N tile");
+    static_assert(S::fits, "shared memory");
+    static_assert(STAGE % 1024 == 0 && A_BYTES % 1024 == 0 && B_BYTES % 512 == 0, "swizzle alignment");
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + NS * STAGE);   // full, split, done [NS]; accf, acce [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3 * NS + 4);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nch = prm.nchunks;
+    const int my_tiles = prm.tiles > (int)blockIdx.x ? (prm.tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int G = my_tiles * nch;
+    auto a_st = [&](int s) { return base + s * STAGE; };
+    auto alo_st = [&](int s) { return base + s * STAGE + A_BYTES; };
+    auto bh_st = [&](int s) { return base + s * STAGE + 2 * A_BYTES; };
+    auto bl_st = [&](int s) { return base + s * STAGE + 2 * A_BYTES + B_BYTES; };
+    const uint32_t full0 = smem_u32(&bars[0]), split0 = smem_u32(&bars[NS]), done0 = smem_u32(&bars[2 * NS]);
+    const uint32_t accf0 = smem_u32(&bars[3 * NS]), acce0 = smem_u32(&bars[3 * NS + 2]);
+
+    if (tid == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(split0 + 8 * s, 128);
+            mbar_init(done0 + 8 * s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(accf0 + 8 * b, 1);
+            mbar_init(acce0 + 8 * b, 128);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 8) {
+        // ---- producer
+        if (lane == 0) {
+            constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
+            for (int g = 0; g < G; ++g) {
+                const int s = g % NS;
+                if (g >= NS && !mbar_wait(done0 + 8 * s, ((g - NS) / NS) & 1)) break;
+                const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x, c = g % nch;
+                mbar_expect_tx(full0 + 8 * s, TX);
+                tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TM, full0 + 8 * s);
+                tma_load_2d(smem_u32(bh_st(s)), &bmap, c * KC, 0, full0 + 8 * s);
+                tma_load_2d(smem_u32(bl_st(s)), &bmap, c * KC, NP, full0 + 8 * s);
+            }
+        }
+    } else if (warp == 9) {
+        // ---- MMA issue
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(NP);
+            for (int g = 0; g < G; ++g) {
+                const int s = g % NS, c = g % nch, t = g / nch, b = t & 1;
+                if (c == 0 && t >= 2 && !mbar_wait(acce0 + 8 * b, ((t - 2) >> 1) & 1)) break;
+                if (!mbar_wait(split0 + 8 * s, (g / NS) & 1)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t ah_a = smem_u32(a_st(s)), al_a = smem_u32(alo_st(s));
+                const uint32_t bh_a = smem_u32(bh_st(s)), bl_a = smem_u32(bl_st(s));
+                const uint32_t d = tmem + (uint32_t)(b * 256);
+#pragma unroll
+                for (int j = 0; j < KC / 8; ++j) {
+                    const uint32_t off = j * 32;   // 8 TF32 = 32 bytes along the 64-byte swizzled row
+                    const uint64_t dah = smem_desc(ah_a + off), dal = smem_desc(al_a + off);
+                    const uint64_t dbh = smem_desc(bh_a + off), dbl = smem_desc(bl_a + off);
+                    mma_tf32(d, dah, dbh, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                    mma_tf32(d, dah, dbl, idesc, 1u);
+                    mma_tf32(d, dal, dbh, idesc, 1u);
+                    mma_tf32(d, dal, dbl, idesc, 1u);
+                }
+                mma_commit(done0 + 8 * s);
+                if (c == nch - 1) mma_commit(accf0 + 8 * b);
+            }
+        }
+    } else if (warp < 4) {
+        // ---- A split: TF32 hi in place, lo into the stage's lo buffer, both rounded to nearest
+        for (int g = 0; g < G; ++g) {
+            const int s = g % NS;
+            if (!mbar_wait(full0 + 8 * s, (g / NS) & 1)) break;
+            float4 *ah = reinterpret_cast<float4 *>(a_st(s));
+            float4 *al = reinterpret_cast<float4 *>(alo_st(s));
+#pragma unroll
+            for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
+                const int e = tid + q * 128;
+                const float4 v = ah[e];
+                const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+                ah[e] = h;
+                al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
+                                    tf32_round(v.w - h.w));
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(split0 + 8 * s);
+        }
+    } else {
+        // ---- epilogue: TMEM -> registers -> global (transposed per plane)
+        const int q = warp & 3;
+        const size_t nstride = (size_t)2 * prm.ldo;
+        for (int t = 0; t < my_tiles; ++t) {
+            const int b = t & 1;
+            if (!mbar_wait(accf0 + 8 * b, (t >> 1) & 1)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int tile = (int)blockIdx.x + t * (int)gridDim.x;
+            const int row = tile * TM + q * 32 + lane;
+            const bool row_ok = row < prm.rows;
+            const int cr = row >> 1, part = row & 1;
+            const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
+            float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
+            const uint32_t tbase = tmem + (uint32_t)(b * 256) + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+            for (int c0 = 0; c0 < NP; c0 += 16) {
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                    "%12, %13, %14, %15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                      "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                      "=r"(v[14]), "=r"(v[15])
+                    : "r"(tbase + (uint32_t)c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row_ok) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int n = c0 + j;
+                        if (n < prm.N) orow[(size_t)n * nstride] = __uint_as_float(v[j]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(acce0 + 8 * b);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -358,10 +541,21 @@ float tf32_round_host(double v) {
 // 256-row tiles where two sub-tiles' stages fit in shared memory (Np <= 192), else 128
 template <int NP> constexpr int sub_tiles() { return TGShape<NP, 2>::fits ? 2 : 1; }
 
+// the warp-specialised kernel unless TDZ_TRANSFORM=split asks for the
+// single-accumulator-pair one
+bool use_ws() {
+    static const bool ws = [] {
+        const char *e = std::getenv("TDZ_TRANSFORM");
+        return !(e && std::string(e) == "split");
+    }();
+    return ws;
+}
+
 template <int NP>
 void launch(const TransformMat &T, const float *in, int ldi, TGParams prm, cudaStream_t st) {
+    const bool ws = use_ws();
     constexpr int MS = sub_tiles<NP>();
-    const size_t smem = TGShape<NP, MS>::SMEM;
+    const size_t smem = ws ? WSShape<NP>::SMEM : TGShape<NP, MS>::SMEM;
     // opt-in to the tile's shared memory once per device (guarded: the batch
     // API steps runs from several host threads)
     {
@@ -371,15 +565,20 @@ void launch(const TransformMat &T, const float *in, int ldi, TGParams prm, cudaS
         TDZ_CUDA(cudaGetDevice(&dev));
         std::lock_guard<std::mutex> lk(mu);
         if (!done.count(dev)) {
-            TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TGShape<NP, MS>::SMEM));
+            TDZ_CUDA(cudaFuncSetAttribute(k_transform_ws<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)WSShape<NP>::SMEM));
             done.insert(dev);
         }
     }
     CUtensorMap amap;
-    make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)(TM * MS));
-    prm.tiles = (prm.rows + TM * MS - 1) / (TM * MS);
+    const int rows_per_tile = ws ? TM : TM * MS;
+    make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)rows_per_tile);
+    prm.tiles = (prm.rows + rows_per_tile - 1) / rows_per_tile;
     const int grid = std::min(prm.tiles, sm_count());
-    k_transform<NP, MS><<<grid, 160, smem, st>>>(amap, T.map, prm);
+    if (ws) k_transform_ws<NP><<<grid, 320, smem, st>>>(amap, T.map, prm);
+    else k_transform<NP, MS><<<grid, 160, smem, st>>>(amap, T.map, prm);
 }
 
 }  // namespace
