@@ -1,5 +1,6 @@
 """Tensor-core plane transform (tcgen05, TF32 with a hi/lo split of both operands)
-against numpy FP64, through the C ABI. Bar: FP32 class, i.e. a max-norm
+against numpy FP64, through the C ABI (the warp-specialised kernel; the
+single-accumulator kernel with TDZ_TRANSFORM=split). Bar: FP32 class, i.e. a max-norm
 relative error at most 4x that of the same contraction evaluated in FP32 by
 numpy (about 1e-6 at K = 163), and never above 1e-5."""
 import ctypes as C
@@ -32,6 +33,7 @@ def _run(K, N, planes, R, ldi, ldo, seed):
 @pytest.mark.gpu
 @pytest.mark.parametrize("K,N,planes,R,ldi,ldo", [
     (163, 163, 5, 163, 164, 164),     # heterostructure inner axis, 5 planes
+    (163, 163, 130, 163, 164, 164),   # 331 row tiles: several per CTA, both TMEM accumulators in turn
     (7, 5, 3, 4, 8, 4),               # tiny, K < one 32-wide chunk, ragged tile
     (40, 256, 2, 70, 40, 72),         # widest N tile, K across two chunks
     (256, 16, 1, 300, 256, 300),      # narrowest N tile, K exactly 8 chunks, 5 M tiles
