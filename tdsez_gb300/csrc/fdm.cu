@@ -1219,12 +1219,8 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
         // [z][y][c][x] -> [z][x'][c][y] -> [z][y'][c][x'] -> line solves -> [z][x][c][y'] -> [z][y][c][x]
         float *a = pa.as<float>(), *b = pb.as<float>();
         const int blocks = (int)std::min<size_t>((N + 255) / 256, (size_t)16 * sm_count());
-        // the first transform reads the natural FP64 input itself where it can
-        if (!transform_from_natural(Tf[0], r, n[2], n[1], b, ldy, st)) {
-            k_to_planar<<<blocks, 256, 0, st>>>(r, a, n[0], rows, ldx);
-            count_launch();
-            transform(Tf[0], a, n[2], n[1], ldx, b, ldy, st);
-        }
+        k_to_planar<<<blocks, 256, 0, st>>>(r, a, n[0], rows, ldx);
+        transform(Tf[0], a, n[2], n[1], ldx, b, ldy, st);
         transform(Tf[1], b, n[2], n[0], ldy, a, ldx, st);
         ZSolveParams zp = line_params(*this);
         zp.x = a;
@@ -1234,13 +1230,10 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
         zp.cs = ldx;
         line_solve(P, zp, st);
         transform(Ti[0], a, n[2], n[1], ldx, b, ldy, st);
-        // the last transform writes the natural FP64 output itself where it can
-        if (!transform_to_natural(Ti[1], b, n[2], n[0], ldy, z, st)) {
-            transform(Ti[1], b, n[2], n[0], ldy, a, ldx, st);
-            k_from_planar<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx);
-            count_launch();
-        }
+        transform(Ti[1], b, n[2], n[0], ldy, a, ldx, st);
+        k_from_planar<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx);
         TDZ_CUDA(cudaGetLastError());
+        count_launch(2);
         ++applies;
         return;
     }

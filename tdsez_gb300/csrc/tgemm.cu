@@ -24,8 +24,6 @@
 // the error word, the consumers leave together, and TMEM is still freed.
 #include "tgemm.h"
 
-#include "cplx.cuh"
-
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -137,7 +135,6 @@ __device__ __forceinline__ float tf32_round(float v) {
 
 struct TGParams {
     float *out;
-    double2 *out64;   // non-null: natural complex FP64 output instead of planar FP32 (warp-specialised kernel)
     int rows;      // GEMM rows = 2 planes R
     int R, N, ldo, nchunks, tiles;
 };
@@ -338,13 +335,9 @@ __global__ void __launch_bounds__(160, 1)
 //   warp 8     (one thread) keeps the stage ring full with TMA.
 // The lo part lives in its stage, so the split of a chunk never waits for
 // MMAs (the producer recycles a stage only after its MMAs completed).
-// IN64: A arrives as natural complex FP64 (64 entries x 16 complex values per
-// chunk, a plain row-major staging tile) and the split warps write the
-// swizzled TF32 hi/lo tiles themselves
-constexpr int STG64_BYTES = (TM / 2) * (2 * KC) * 8;   // 16 KB
-template <int NP, bool IN64 = false> struct WSShape {
+template <int NP> struct WSShape {
     static constexpr int B_BYTES = NP * KC * 4;
-    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES + (IN64 ? STG64_BYTES : 0);   // A hi, A lo, B hi, B lo[, A FP64]
+    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;   // A (hi in place), A lo, B hi, B lo
     static constexpr size_t smem_for(int ns) { return 1024 + (size_t)ns * STAGE + (3 * ns + 4) * 8 + 16; }
     static constexpr int NS = smem_for(6) <= 232448   ? 6
                               : smem_for(5) <= 232448 ? 5
@@ -355,18 +348,11 @@ template <int NP, bool IN64 = false> struct WSShape {
     static constexpr bool fits = SMEM <= 232448;
 };
 
-// byte offset of element (row, k) in a 64-byte-swizzled K-major tile of
-// 64-byte rows (what TMA's 64-byte swizzle writes and the MMA descriptor
-// reads): the 16-byte chunk index is XORed with bits 1-2 of the row
-__device__ __forceinline__ uint32_t swz64(int row, int k) {
-    return (uint32_t)(row * 64 + ((((k >> 2) ^ (row >> 1)) & 3) << 4) + ((k & 3) << 2));
-}
-
-template <int NP, bool IN64>
+template <int NP>
 __global__ void __launch_bounds__(320, 1)
     k_transform_ws(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                    const TGParams prm) {
-    using S = WSShape<NP, IN64>;
+    using S = WSShape<NP>;
     constexpr int NS = S::NS, STAGE = S::STAGE, B_BYTES = S::B_BYTES;
     constexpr uint32_t TMEM_COLS = 512;   // two accumulators, columns 0 and 256
     static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N tile");
@@ -384,7 +370,6 @@ __global__ void __launch_bounds__(320, 1)
     auto alo_st = [&](int s) { return base + s * STAGE + A_BYTES; };
     auto bh_st = [&](int s) { return base + s * STAGE + 2 * A_BYTES; };
     auto bl_st = [&](int s) { return base + s * STAGE + 2 * A_BYTES + B_BYTES; };
-    auto stg_st = [&](int s) { return base + s * STAGE + 2 * A_BYTES + 2 * B_BYTES; };
     const uint32_t full0 = smem_u32(&bars[0]), split0 = smem_u32(&bars[NS]), done0 = smem_u32(&bars[2 * NS]);
     const uint32_t accf0 = smem_u32(&bars[3 * NS]), acce0 = smem_u32(&bars[3 * NS + 2]);
 
@@ -414,16 +399,13 @@ __global__ void __launch_bounds__(320, 1)
     if (warp == 8) {
         // ---- producer
         if (lane == 0) {
-            constexpr uint32_t TX = (IN64 ? STG64_BYTES : A_BYTES) + 2 * B_BYTES;
+            constexpr uint32_t TX = A_BYTES + 2 * B_BYTES;
             for (int g = 0; g < G; ++g) {
                 const int s = g % NS;
                 if (g >= NS && !mbar_wait(done0 + 8 * s, ((g - NS) / NS) & 1)) break;
                 const int tile = (int)blockIdx.x + (g / nch) * (int)gridDim.x, c = g % nch;
                 mbar_expect_tx(full0 + 8 * s, TX);
-                if constexpr (IN64)   // 64 natural rows x 32 doubles (16 complex values) at x = 16 c
-                    tma_load_2d(smem_u32(stg_st(s)), &amap, c * 2 * KC, tile * (TM / 2), full0 + 8 * s);
-                else
-                    tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TM, full0 + 8 * s);
+                tma_load_2d(smem_u32(a_st(s)), &amap, c * KC, tile * TM, full0 + 8 * s);
                 tma_load_2d(smem_u32(bh_st(s)), &bmap, c * KC, 0, full0 + 8 * s);
                 tma_load_2d(smem_u32(bl_st(s)), &bmap, c * KC, NP, full0 + 8 * s);
             }
@@ -463,35 +445,16 @@ __global__ void __launch_bounds__(320, 1)
         for (int g = 0; g < G; ++g) {
             const int s = g % NS;
             if (!mbar_wait(full0 + 8 * s, (g / NS) & 1)) break;
-            if constexpr (IN64) {
-                // entry j, value k (complex FP64) -> rows 2j (real) and 2j + 1 (imaginary),
-                // column k: rounded to FP32 as the planar path does, then split
-                const double2 *stg = reinterpret_cast<const double2 *>(stg_st(s));
-                uint8_t *ah = a_st(s), *al = alo_st(s);
+            float4 *ah = reinterpret_cast<float4 *>(a_st(s));
+            float4 *al = reinterpret_cast<float4 *>(alo_st(s));
 #pragma unroll
-                for (int q = 0; q < (TM / 2) * KC / 128; ++q) {
-                    const int e = tid + q * 128, j = e / KC, k = e % KC;
-                    const double2 v = stg[j * KC + k];
-                    const dff re = dff_split(v.x), im = dff_split(v.y);
-                    const float vr = __fadd_rn(re.hi, re.lo), vi = __fadd_rn(im.hi, im.lo);
-                    const float hr = tf32_round(vr), hi_ = tf32_round(vi);
-                    *reinterpret_cast<float *>(ah + swz64(2 * j, k)) = hr;
-                    *reinterpret_cast<float *>(ah + swz64(2 * j + 1, k)) = hi_;
-                    *reinterpret_cast<float *>(al + swz64(2 * j, k)) = tf32_round(vr - hr);
-                    *reinterpret_cast<float *>(al + swz64(2 * j + 1, k)) = tf32_round(vi - hi_);
-                }
-            } else {
-                float4 *ah = reinterpret_cast<float4 *>(a_st(s));
-                float4 *al = reinterpret_cast<float4 *>(alo_st(s));
-#pragma unroll
-                for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
-                    const int e = tid + q * 128;
-                    const float4 v = ah[e];
-                    const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
-                    ah[e] = h;
-                    al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
-                                        tf32_round(v.w - h.w));
-                }
+            for (int q = 0; q < A_BYTES / 16 / 128; ++q) {
+                const int e = tid + q * 128;
+                const float4 v = ah[e];
+                const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+                ah[e] = h;
+                al[e] = make_float4(tf32_round(v.x - h.x), tf32_round(v.y - h.y), tf32_round(v.z - h.z),
+                                    tf32_round(v.w - h.w));
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(split0 + 8 * s);
@@ -511,8 +474,6 @@ __global__ void __launch_bounds__(320, 1)
             const int p = row_ok ? cr / prm.R : 0, r = row_ok ? cr % prm.R : 0;
             float *orow = prm.out + ((size_t)p * prm.N * 2 + part) * prm.ldo + r;
             const uint32_t tbase = tmem + (uint32_t)(b * 256) + ((uint32_t)(q * 32) << 16);
-            // natural FP64 output: lanes 2k and 2k + 1 hold the two parts of one entry
-            double2 *nrow = prm.out64 ? prm.out64 + (size_t)p * prm.N * prm.R + r : nullptr;
 #pragma unroll 1
             for (int c0 = 0; c0 < NP; c0 += 16) {
                 uint32_t v[16];
@@ -524,16 +485,7 @@ __global__ void __launch_bounds__(320, 1)
                       "=r"(v[14]), "=r"(v[15])
                     : "r"(tbase + (uint32_t)c0));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (nrow) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const float mine = __uint_as_float(v[j]);
-                        const float other = __shfl_xor_sync(0xffffffffu, mine, 1);
-                        const int n = c0 + j;
-                        if (row_ok && part == 0 && n < prm.N)
-                            nrow[(size_t)n * prm.R] = make_double2(f2d_exact(mine), f2d_exact(other));
-                    }
-                } else if (row_ok) {
+                if (row_ok) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int n = c0 + j;
@@ -603,26 +555,12 @@ bool use_ws() {
     return ws;
 }
 
-// 2D FP64 tensor map of natural complex rows: `rows` rows of n complex values
-// (pitch n), box 2 KC doubles x TM / 2 rows, no swizzle, zero fill outside
-void make_map64(CUtensorMap *map, const void *ptr, uint64_t n, uint64_t rows) {
-    TDZ_CHECK((reinterpret_cast<uintptr_t>(ptr) & 15) == 0, TDZ_ERR_ARG, "transform operand not 16-byte aligned");
-    const cuuint64_t dims[2] = {2 * n, rows};
-    const cuuint64_t strides[1] = {2 * n * 8};
-    const cuuint32_t box[2] = {(cuuint32_t)(2 * KC), (cuuint32_t)(TM / 2)};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void *>(ptr), dims, strides,
-                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    TDZ_CHECK(r == CUDA_SUCCESS, TDZ_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-}
-
-// in64: natural complex FP64 input (rows of K complex values), else row-planar FP32 (pitch ldi)
 template <int NP>
-void launch(const TransformMat &T, const void *in, bool in64, int ldi, TGParams prm, cudaStream_t st) {
-    const bool ws = use_ws() || in64;
+void launch(const TransformMat &T, const float *in, int ldi, TGParams prm, cudaStream_t st) {
+    const bool ws = use_ws();
     constexpr int MS = sub_tiles<NP>();
-    // opt-in to the kernels' shared memory once per device (guarded: the batch
+    const size_t smem = ws ? WSShape<NP>::SMEM : TGShape<NP, MS>::SMEM;
+    // opt-in to the tile's shared memory once per device (guarded: the batch
     // API steps runs from several host threads)
     {
         static std::mutex mu;
@@ -633,22 +571,18 @@ void launch(const TransformMat &T, const void *in, bool in64, int ldi, TGParams 
         if (!done.count(dev)) {
             TDZ_CUDA(cudaFuncSetAttribute(k_transform<NP, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)TGShape<NP, MS>::SMEM));
-            TDZ_CUDA(cudaFuncSetAttribute(k_transform_ws<NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)WSShape<NP, false>::SMEM));
-            TDZ_CUDA(cudaFuncSetAttribute(k_transform_ws<NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)WSShape<NP, true>::SMEM));
+            TDZ_CUDA(cudaFuncSetAttribute(k_transform_ws<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)WSShape<NP>::SMEM));
             done.insert(dev);
         }
     }
     CUtensorMap amap;
     const int rows_per_tile = ws ? TM : TM * MS;
-    if (in64) make_map64(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows / 2);
-    else make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)rows_per_tile);
+    make_map(&amap, in, (uint64_t)T.K, (uint64_t)prm.rows, (uint64_t)ldi, (uint32_t)rows_per_tile);
     prm.tiles = (prm.rows + rows_per_tile - 1) / rows_per_tile;
     const int grid = std::min(prm.tiles, sm_count());
-    if (in64) k_transform_ws<NP, true><<<grid, 320, WSShape<NP, true>::SMEM, st>>>(amap, T.map, prm);
-    else if (ws) k_transform_ws<NP, false><<<grid, 320, WSShape<NP, false>::SMEM, st>>>(amap, T.map, prm);
-    else k_transform<NP, MS><<<grid, 160, TGShape<NP, MS>::SMEM, st>>>(amap, T.map, prm);
+    if (ws) k_transform_ws<NP><<<grid, 320, smem, st>>>(amap, T.map, prm);
+    else k_transform<NP, MS><<<grid, 160, smem, st>>>(amap, T.map, prm);
 }
 
 }  // namespace
@@ -684,68 +618,39 @@ int take_transform_error() {
     return h;
 }
 
-namespace {
-void transform_impl(const TransformMat &T, const void *in, bool in64, int planes, int R, int ldi, float *out,
-                    double2 *out64, int ldo, cudaStream_t st);
-}  // namespace
-
 void transform(const TransformMat &T, const float *in, int planes, int R, int ldi, float *out, int ldo,
                cudaStream_t st) {
-    transform_impl(T, in, false, planes, R, ldi, out, nullptr, ldo, st);
-}
-
-bool transform_from_natural(const TransformMat &T, const double2 *in64, int planes, int R, float *out, int ldo,
-                            cudaStream_t st) {
-    if (!use_ws()) return false;
-    transform_impl(T, in64, true, planes, R, T.K, out, nullptr, ldo, st);
-    return true;
-}
-
-bool transform_to_natural(const TransformMat &T, const float *in, int planes, int R, int ldi, double2 *out64,
-                          cudaStream_t st) {
-    if (!use_ws()) return false;
-    TDZ_CHECK((reinterpret_cast<uintptr_t>(out64) & 15) == 0, TDZ_ERR_ARG, "FP64 output not 16-byte aligned");
-    transform_impl(T, in, false, planes, R, ldi, nullptr, out64, R, st);
-    return true;
-}
-
-namespace {
-void transform_impl(const TransformMat &T, const void *in, bool in64, int planes, int R, int ldi, float *out,
-                    double2 *out64, int ldo, cudaStream_t st) {
     TDZ_CHECK(ldi >= T.K && ldo >= R, TDZ_ERR_ARG, "transform pitches too small");
     const long long rows = 2LL * planes * R;
     TDZ_CHECK(rows < (1LL << 31), TDZ_ERR_ARG, "transform too large");
     TGParams prm{};
     prm.out = out;
-    prm.out64 = out64;
     prm.rows = (int)rows;
     prm.R = R;
     prm.N = T.N;
     prm.ldo = ldo;
     prm.nchunks = T.Kp / KC;
     switch (T.Np) {
-    case 16: launch<16>(T, in, in64, ldi, prm, st); break;
-    case 32: launch<32>(T, in, in64, ldi, prm, st); break;
-    case 48: launch<48>(T, in, in64, ldi, prm, st); break;
-    case 64: launch<64>(T, in, in64, ldi, prm, st); break;
-    case 80: launch<80>(T, in, in64, ldi, prm, st); break;
-    case 96: launch<96>(T, in, in64, ldi, prm, st); break;
-    case 112: launch<112>(T, in, in64, ldi, prm, st); break;
-    case 128: launch<128>(T, in, in64, ldi, prm, st); break;
-    case 144: launch<144>(T, in, in64, ldi, prm, st); break;
-    case 160: launch<160>(T, in, in64, ldi, prm, st); break;
-    case 176: launch<176>(T, in, in64, ldi, prm, st); break;
-    case 192: launch<192>(T, in, in64, ldi, prm, st); break;
-    case 208: launch<208>(T, in, in64, ldi, prm, st); break;
-    case 224: launch<224>(T, in, in64, ldi, prm, st); break;
-    case 240: launch<240>(T, in, in64, ldi, prm, st); break;
-    case 256: launch<256>(T, in, in64, ldi, prm, st); break;
+    case 16: launch<16>(T, in, ldi, prm, st); break;
+    case 32: launch<32>(T, in, ldi, prm, st); break;
+    case 48: launch<48>(T, in, ldi, prm, st); break;
+    case 64: launch<64>(T, in, ldi, prm, st); break;
+    case 80: launch<80>(T, in, ldi, prm, st); break;
+    case 96: launch<96>(T, in, ldi, prm, st); break;
+    case 112: launch<112>(T, in, ldi, prm, st); break;
+    case 128: launch<128>(T, in, ldi, prm, st); break;
+    case 144: launch<144>(T, in, ldi, prm, st); break;
+    case 160: launch<160>(T, in, ldi, prm, st); break;
+    case 176: launch<176>(T, in, ldi, prm, st); break;
+    case 192: launch<192>(T, in, ldi, prm, st); break;
+    case 208: launch<208>(T, in, ldi, prm, st); break;
+    case 224: launch<224>(T, in, ldi, prm, st); break;
+    case 240: launch<240>(T, in, ldi, prm, st); break;
+    case 256: launch<256>(T, in, ldi, prm, st); break;
     default: throw Error(TDZ_ERR_INTERNAL, "bad transform tile width");
     }
     TDZ_CUDA(cudaGetLastError());
     count_launch();
 }
-
-}  // namespace
 
 }  // namespace tdz

@@ -39,16 +39,5 @@ int take_transform_error();
 
 void transform(const TransformMat &T, const float *in, int planes, int R, int ldi, float *out, int ldo,
                cudaStream_t st);
-// The same transform with the result written as natural complex FP64,
-// out64[(p N + n) R + r] = (part 0, part 1) of out[p][n][.][r] (the FDM
-// output without a separate layout pass). Returns false, doing nothing, when
-// the kernel in use cannot write it (TDZ_TRANSFORM=split).
-bool transform_to_natural(const TransformMat &T, const float *in, int planes, int R, int ldi, double2 *out64,
-                          cudaStream_t st);
-// The same transform reading natural complex FP64 input rows (in64[(p R + r)
-// K + k], K = T.K; rounded to FP32 as the planar layout pass does) and
-// writing the planar FP32 result; false when unavailable (TDZ_TRANSFORM=split).
-bool transform_from_natural(const TransformMat &T, const double2 *in64, int planes, int R, float *out, int ldo,
-                            cudaStream_t st);
 
 }  // namespace tdz
