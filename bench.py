@@ -167,7 +167,7 @@ def batch_scan(args):
         psi = op.separable_state([lambda x: np.exp(-x * x / 2.0)] * 2)
         runs.append((S, op, field, psi, nel, p))
     def make():
-        return [Propagator(op, "cn", field=f, pc="mg", precision="fp32", rtol=1e-10, outer="df")
+        return [Propagator(op, "cn", field=f, pc=args.scan_pc, precision="fp32", rtol=1e-10, outer="df")
                 for (S, op, f, psi, nel, p) in runs]
     dt = 0.05
     steps = args.steps
@@ -195,8 +195,10 @@ def batch_scan(args):
     torch.cuda.synchronize()
     t_batch = time.time() - t0
     n = len(runs)
+    its = sum(G.stats()["its"] for G in Pb) / max(1, sum(G.stats()["solves"] for G in Pb))
     print(json.dumps({"metric": "batched 2D soft-core scan, CN run-steps/s", "value": n * steps / t_batch,
                       "unit": "run-steps/s", "serial": n * steps / t_serial, "speedup": t_serial / t_batch,
+                      "preconditioner": args.scan_pc, "its_per_solve": its,
                       "runs": n, "steps": steps, "threads": args.scan_threads,
                       "grids": sorted(set(int(r[4]) for r in runs)), "degrees": sorted(set(int(r[5]) for r in runs)),
                       "ndof_total": int(sum(r[0].ndof for r in runs)),
@@ -680,6 +682,7 @@ def main():
     ap.add_argument("--precond-only", action="store_true")
     ap.add_argument("--batch-scan", type=int, default=0, help="runs of the batched 2D scan (0: headline bench)")
     ap.add_argument("--scan-min-el", type=int, default=128)
+    ap.add_argument("--scan-pc", default="fdm", choices=["fdm", "mg"], help="preconditioner of the scan's runs")
     ap.add_argument("--scan-max-el", type=int, default=512)
     ap.add_argument("--scan-threads", type=int, default=16)
     ap.add_argument("--mg-smooth", type=int, default=8)
