@@ -804,20 +804,27 @@ __global__ void __launch_bounds__(2 * kZ2Lines) k_zsolve2(const ZSolveParams prm
 }
 
 template <int P, bool CI> void launch_zsolve_t(const ZSolveParams &zp, cudaStream_t st) {
+    constexpr size_t kMax = 220 * 1024;
+    // the dynamic shared-memory limit is a property of the kernel, not of a
+    // launch: set it once to the largest size any line length may use, so
+    // that solves of different lengths from several host threads cannot
+    // lower it under each other's launches
+    static const bool attr = [] {
+        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve2<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax));
+        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax));
+        return true;
+    }();
+    (void)attr;
     const int nl = zp.n0 * zp.n1;
     k_zbands<<<(zp.n2 * (2 * P + 1) + 255) / 256, 256, 0, st>>>(zp, 2 * P + 1);
     if (zp.n2 >= 4 * ZBlk2<P>::B) {
         const size_t smem = zsolve2_smem<P>(zp.n2);
-        TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
-        if (smem > 48 * 1024)
-            TDZ_CUDA(cudaFuncSetAttribute(k_zsolve2<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        TDZ_CHECK(smem <= kMax, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
         k_zsolve2<P, CI><<<(nl + kZ2Lines - 1) / kZ2Lines, 2 * kZ2Lines, smem, st>>>(zp);
         return;
     }
     const size_t smem = zsolve_smem<P>(zp.n2);
-    TDZ_CHECK(smem <= 220 * 1024, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
-    if (smem > 48 * 1024)
-        TDZ_CUDA(cudaFuncSetAttribute(k_zsolve<P, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TDZ_CHECK(smem <= kMax, TDZ_ERR_UNSUPPORTED, "outer axis too long for the FDM line solve");
     k_zsolve<P, CI><<<(nl + kZThreads - 1) / kZThreads, kZThreads, smem, st>>>(zp);
 }
 

@@ -145,8 +145,13 @@ void run_axis(const T *L, int axis, typename CT<T>::type *x, int n0, int n1, int
         while (rows > 1 && (size_t)rows * n0 * sizeof(C) > 96 * 1024) rows /= 2;
         const size_t smem = (size_t)rows * n0 * sizeof(C);
         TDZ_CHECK(smem <= 200 * 1024, TDZ_ERR_UNSUPPORTED, "axis too long for the row line solve");
-        if (smem > 48 * 1024)
-            TDZ_CUDA(cudaFuncSetAttribute(k_line_rows<T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // set once to the largest size (a per-kernel limit: concurrent solves of
+        // other lengths must not lower it under this launch)
+        static const bool attr = [] {
+            TDZ_CUDA(cudaFuncSetAttribute(k_line_rows<T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            return true;
+        }();
+        (void)attr;
         const int nrows = n1 * n2;
         k_line_rows<T, P><<<(nrows + rows - 1) / rows, rows, smem, st>>>(L, n0, x, nrows);
     } else if (axis == 1) {
