@@ -50,3 +50,40 @@ def test_batch_equals_serial(cuda):
         assert np.linalg.norm(a - b) <= 1e-10 * np.linalg.norm(a)
     for G, _ in batch:
         assert G.stats()["solves"] == 3
+
+
+@pytest.mark.gpu
+def test_batch_fdm_ragged_outer_axes(cuda):
+    """FDM-preconditioned 2D runs whose outer axes have different lengths
+    (degree 5, 240 to 300 elements: line solves with different, large
+    shared-memory footprints), stepped together from the thread pool: the
+    same states as stepping them one by one."""
+    import torch
+    from oracle import bspline as ob
+    from tdsez_gb300.operators import Operator, Physics
+    from tdsez_gb300.propagator import BatchPropagator, Propagator
+    from tdsez_gb300.space import Space
+
+    def make():
+        out = []
+        for k, nel in enumerate((240, 260, 280, 300)):
+            p = 5
+            S = Space([ob.uniform_knots(16, -12.0, 12.0, p), ob.uniform_knots(nel, -60.0, 60.0, p)], p, 6)
+            op = Operator(S, Physics(charge=-1.0, mass=1.0, coupled=(0,), softcore=[(1.0, 0.0, 0.0, 0.0, 1.0)]))
+            E0 = 0.02 * (k + 1)
+            G = Propagator(op, "cn", field=(lambda E0: (lambda t: [E0 * math.sin(0.3 * t)]))(E0), pc="fdm",
+                           precision="fp32", rtol=1e-11, outer="df")
+            psi = op.separable_state([lambda x: np.exp(-x * x / 4.0), lambda y: np.exp(-y * y / 8.0)])
+            out.append((G, psi))
+        return out
+    serial, batch = make(), make()
+    B = BatchPropagator([G for G, _ in batch], threads=4)
+    psis = [p for _, p in batch]
+    for step in range(3):
+        for G, p in serial:
+            G.step(p, step * 0.05, 0.05)
+        B.step(psis, step * 0.05, 0.05)
+    torch.cuda.synchronize()
+    for (Gs, ps), pb in zip(serial, psis):
+        a, b = ps.cpu().numpy(), pb.cpu().numpy()
+        assert np.linalg.norm(a - b) <= 1e-10 * np.linalg.norm(a)
