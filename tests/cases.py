@@ -71,6 +71,16 @@ def _c3c():
                 bounds=[(-18.0, 18.0), (-16.0, 16.0)])
 
 
+@case("3d_cap_free")
+def _c3d_cap_free():
+    """Free carrier in 3D with absorbing layers on every axis (t-SURFF end term)."""
+    p, nq = 3, 4
+    knots = [ob.uniform_knots(9, -12.0, 12.0, p), ob.uniform_knots(8, -11.0, 11.0, p),
+             ob.uniform_knots(10, -13.0, 13.0, p)]
+    return dict(knots=knots, p=p, nq=nq, charge=-1.0, mass=1.0, V=[None, None, None], coupled=(2,), cap_kmin=1.2,
+                bounds=[(-12.0, 12.0), (-11.0, 11.0), (-13.0, 13.0)])
+
+
 @case("3d_heterostructure")
 def _c4():
     p, nq = 3, 4

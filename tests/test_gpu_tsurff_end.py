@@ -4,7 +4,7 @@ preconditioner it uses in 1D, through the C ABI:
 * the banded LU inverts 1D stage operators (absorbing layer, walls, layered
   mass) exactly: FGMRES converges in one iteration to the direct solution;
 * end-term amplitudes equal the oracle's (one direct sparse solve per energy
-  node) on the same states, in 1D and 2D;
+  node) on the same states, in 1D, 2D and 3D;
 * the reference's END1D acceptance case run entirely on the GPU: the end
   term restores the analytic spectrum of a packet stopped inside the box;
 * the guards: the field must be over at T, the operator must carry the
@@ -77,6 +77,7 @@ def _packet(S, c, k0, width=1.0):
 @pytest.mark.parametrize("name,R,kg,dp", [
     ("1d_cap_free", 5.0, [(-1.0, 2.5, 15)], 0.0),
     ("2d_cap_free", 6.0, [(-0.5, 2.0, 6), (-1.0, 1.5, 5)], 0.12),
+    ("3d_cap_free", 4.0, [(-0.5, 1.0, 3), (-0.5, 1.0, 3), (-0.2, 1.2, 4)], 0.25),
 ])
 def test_end_term_parity(cuda, name, R, kg, dp):
     """Same states sampled by both, then the end term: GPU (FGMRES per node,
@@ -87,7 +88,7 @@ def test_end_term_parity(cuda, name, R, kg, dp):
     S, ph, _ = oracle_of(c)
     PS, op = product_of(c)
     dim = S.dim
-    psi, A = _packet(S, c, [1.2, 0.6][:dim])
+    psi, A = _packet(S, c, [1.2, 0.6, 0.9][:dim])
     field3 = lambda t: [_pulse(t), 0.0, 0.0]
     dt = 0.1
     ks = [np.linspace(*k) for k in kg]
