@@ -209,11 +209,13 @@ def end_nodes(pmin, pmax, split, dp_in, dp_out):
     node = []
 
     def segment(a, b, dp):
+        # the last node is b itself: one rounding below it would open a second
+        # segment with a node next to it (Lagrange weights over the difference)
         if not b > a:
             return
         cnt = max(1, int(math.ceil((b - a) / dp - 1e-9)))
         for i in range(0 if not node else 1, cnt + 1):
-            node.append(a + (b - a) * i / cnt)
+            node.append(b if i == cnt else a + (b - a) * i / cnt)
     segment(pmin, split, dp_in)
     segment(node[-1] if node else pmin, pmax, dp_out)
     while len(node) < 4:

@@ -45,10 +45,13 @@ namespace {
 std::vector<double> energy_nodes(double pmin, double pmax, double split, double dp_in, double dp_out) {
     std::vector<double> node;
     if (!(pmax > pmin)) return {pmin};
+    // a segment ends exactly at b: a last node a + (b - a) cnt / cnt one
+    // rounding below b would open a second segment of one node next to it,
+    // whose Lagrange weights divide by the rounding difference
     auto segment = [&](double a, double b, double dp) {
         if (!(b > a)) return;
         const int cnt = std::max(1, (int)std::ceil((b - a) / dp - 1e-9));
-        for (int i = node.empty() ? 0 : 1; i <= cnt; ++i) node.push_back(a + (b - a) * i / cnt);
+        for (int i = node.empty() ? 0 : 1; i <= cnt; ++i) node.push_back(i == cnt ? b : a + (b - a) * i / cnt);
     };
     segment(pmin, split, dp_in);
     segment(node.empty() ? pmin : node.back(), pmax, dp_out);

@@ -53,6 +53,10 @@ def test_end_nodes_rule():
     d = np.diff(n)
     assert np.all(d > 0)
     assert np.allclose(d[n[:-1] < 1.0 - 1e-12], 0.9 / 90) and np.allclose(d[n[:-1] >= 1.0 - 1e-12], 2.0 / 40)
+    # each segment ends exactly at its end: no near-duplicate node when the split is p_max
+    for pmax in (1.8411387545741371, 1.0 + 1e-13, 0.7 + 3 * 0.1):
+        n = ots.end_nodes(0.3910663495531109, pmax, pmax, 0.25, 0.25)
+        assert n[-1] == pmax and np.all(np.diff(n) > 1e-6)
     # too few nodes: midpoints until there are four
     assert len(ots.end_nodes(1.0, 1.1, 1.0, 1.0, 1.0)) == 5
     assert len(ots.end_nodes(2.0, 2.0, 2.0, 0.1, 0.1)) == 1
