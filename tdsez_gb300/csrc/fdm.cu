@@ -251,6 +251,44 @@ __global__ void k_to_planar(const double2 *__restrict__ r, float *__restrict__ a
     }
 }
 
+// the same with ||z||^2: FP32 sums per thread (a few dozen squares of FP32
+// values), FP64 per block into part[block]
+__global__ void __launch_bounds__(256) k_from_planar_norm(const float *__restrict__ a, double2 *__restrict__ z, int n0,
+                                                          size_t rows, int ld, double *__restrict__ part) {
+    const size_t total = rows * (size_t)n0;
+    float acc = 0.f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = e / n0;
+        const int x = (int)(e % n0);
+        const float re = a[(row * 2) * ld + x], im = a[(row * 2 + 1) * ld + x];
+        z[e] = make_double2(f2d_exact(re), f2d_exact(im));
+        acc = fmaf(re, re, fmaf(im, im, acc));
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = (double)acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// *out = sum of part[0 .. n) in a fixed order (one block)
+__global__ void __launch_bounds__(256) k_sum_parts(const double *__restrict__ part, int n, double *out) {
+    __shared__ double ws[256];
+    double t = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) t += part[i];
+    ws[threadIdx.x] = t;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) ws[threadIdx.x] += ws[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = ws[0];
+}
+
 __global__ void k_from_planar(const float *__restrict__ a, double2 *__restrict__ z, int n0, size_t rows, int ld) {
     const size_t total = rows * (size_t)n0;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -997,6 +1035,7 @@ void PcFDM::setup(Operator *op_, int prec) {
     ufac.alloc(zsolve_state_size(P, n[dim - 1], N / n[dim - 1]) * sizeof(float2));
     zb.alloc((size_t)2 * n[dim - 1] * (2 * P + 1) * sizeof(float2));
     if (tensor) {
+        npart.alloc((size_t)16 * sm_count() * sizeof(double));
         ldx = (n[0] + 3) / 4 * 4;
         ldy = (n[1] + 3) / 4 * 4;
         pa.alloc((size_t)n[2] * n[1] * 2 * ldx * sizeof(float));
@@ -1220,6 +1259,13 @@ void line_solve(int P, const ZSolveParams &zp, cudaStream_t st) {
 
 }  // namespace
 
+void PcFDM::apply_norm(const double2 *r, double2 *z, double *norm2, cudaStream_t st) {
+    TDZ_CHECK(tensor, TDZ_ERR_INTERNAL, "fused norm only on the tensor-core path");
+    norm_out = norm2;
+    apply(r, z, st);
+    norm_out = nullptr;
+}
+
 void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
     const size_t rows = (size_t)n[1] * n[2];
     if (tensor) {
@@ -1238,7 +1284,13 @@ void PcFDM::apply(const double2 *r, double2 *z, cudaStream_t st) {
         line_solve(P, zp, st);
         transform(Ti[0], a, n[2], n[1], ldx, b, ldy, st);
         transform(Ti[1], b, n[2], n[0], ldy, a, ldx, st);
-        k_from_planar<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx);
+        if (norm_out) {
+            k_from_planar_norm<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx, npart.as<double>());
+            k_sum_parts<<<1, 256, 0, st>>>(npart.as<double>(), blocks, norm_out);
+            count_launch();
+        } else {
+            k_from_planar<<<blocks, 256, 0, st>>>(a, z, n[0], rows, ldx);
+        }
         TDZ_CUDA(cudaGetLastError());
         count_launch(2);
         ++applies;

@@ -59,8 +59,13 @@ struct PcFDM : Precond {
     bool f64 = false;          // FP64 preconditioner: SIMT FP64 transforms and FP64 line solves
                                // (partial pivoting; factors in ufac, interchanges in piv64)
     DevBuf piv64;
+    DevBuf npart;              // per-block partial sums of ||z||^2 (apply_norm)
+    double *norm_out = nullptr;   // set during apply_norm
     void setup(Operator *op_, int prec = TDZ_FP32);
     void apply(const double2 *r, double2 *z, cudaStream_t st) override;
+    // the tensor-core path forms ||z||^2 in its output layout pass
+    bool has_apply_norm() const override { return tensor; }
+    void apply_norm(const double2 *r, double2 *z, double *norm2, cudaStream_t st) override;
 };
 
 }  // namespace tdz

@@ -36,6 +36,7 @@ void FGMRES::setup(Operator *op_, int restart_, Precond *pc_) {
     if (relaxed) {
         z32.alloc(n * sizeof(float2));
         w32.alloc(n * sizeof(float2));
+        znd.alloc(restart * sizeof(double));
     }
     red.init();
 }
@@ -63,6 +64,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
     std::vector<cd> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), h(m + 1), h2(m + 1), y(m);
     std::vector<cd> dts(m + 1), hc(m + 1), yc(m);
     std::vector<double> zn(m, 0.0);     // ||z_j|| (units of H) of relaxed columns, 0 for exact ones
+    std::vector<char> zn_dev(m, 0);     // ||z_j||^2 still on the device (znd[j])
     // the relaxed error bound's constant for this stage: gamma || |A| ||
     const bool f32m64 = op->f32_on_f64();
     const double relax_c = relaxed ? fp32_apply_gamma(op->P) * op->abs_norm_bound(TDZ_STAGE) : 0.0;
@@ -102,7 +104,12 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         for (; j < m && total < maxit; ++j) {
             ++total;
             double2 *zj = Z[j].as<double2>();
-            pc->apply(V[j].as<double2>(), zj, st);
+            // the relaxed bound needs ||z_j||: from the preconditioner's own output
+            // pass where it can, read back with the cycle's other host values
+            const bool fuse_zn = relax && f32m64 && pc->has_apply_norm();
+            if (fuse_zn) pc->apply_norm(V[j].as<double2>(), zj, znd.as<double>() + j, st);
+            else pc->apply(V[j].as<double2>(), zj, st);
+            zn_dev[j] = fuse_zn;
             double2 *wv = w.as<double2>();
             const double ws = j == 0 ? beta : 1.0;   // stored w = ws A z_j
             bool have_dots = false;
@@ -119,7 +126,7 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
                     op->apply(TDZ_STAGE, TDZ_FP32, z32.ptr, w32.ptr, st);
                     blas::cast(w32.ptr, TDZ_FP32, wv, TDZ_FP64, n, st);
                 }
-                zn[j] = blas::nrm2(red, zj, n, TDZ_FP64, st);
+                if (!fuse_zn) zn[j] = blas::nrm2(red, zj, n, TDZ_FP64, st);
                 ++relaxed_applies;
                 used_relaxed = true;
             } else if (j == 0) {
@@ -230,8 +237,20 @@ SolveStats FGMRES::solve(const double2 *b, double2 *x, double rtol, int maxit, c
         // relaxed applies: the bound on the gap between the estimate and the
         // true residual of this cycle, sum_j |y_j| gamma || |A| || ||z_j||
         double gap = 0.0;
-        if (used_relaxed)
+        if (used_relaxed) {
+            bool any = false;
+            for (int i = 0; i < k; ++i) any = any || zn_dev[i];
+            if (any) {
+                std::vector<double> h2v(k);
+                TDZ_CUDA(cudaMemcpyAsync(h2v.data(), znd.ptr, k * sizeof(double), cudaMemcpyDeviceToHost, st));
+                TDZ_CUDA(cudaStreamSynchronize(st));
+                // the pass sums |z|^2 of FP32 values in FP32 per thread: a relative
+                // error far below 1e-5, covered by the margin
+                for (int i = 0; i < k; ++i)
+                    if (zn_dev[i]) zn[i] = std::sqrt(std::max(h2v[i], 0.0)) * (1.0 + 1e-5);
+            }
             for (int i = 0; i < k; ++i) gap += std::abs(y[i]) * relax_c * zn[i];
+        }
         const bool certified = done && s.rnorm <= target && (!used_relaxed || s.rnorm + gap <= target);
         const bool final_one = cn_psi && k == 1 && certified && s.reason != -9;
         if (final_one) {

@@ -16,6 +16,10 @@ struct Precond {
     virtual void apply(const double2 *r, double2 *z, cudaStream_t st) = 0;
     virtual void refresh() {}   // rebuild from the current stage operator
     virtual long long launches() const { return 0; }
+    // z = P^-1 r and ||z||^2 into *norm2 (device), in the pass that writes z,
+    // where the preconditioner can (has_apply_norm)
+    virtual bool has_apply_norm() const { return false; }
+    virtual void apply_norm(const double2 *r, double2 *z, double *norm2, cudaStream_t st) { apply(r, z, st); }
 };
 
 struct PcNone : Precond {
@@ -42,6 +46,7 @@ struct FGMRES {
     Precond *pc = nullptr;
     std::vector<DevBuf> V, Z;
     DevBuf w;
+    DevBuf znd;                 // ||z_j||^2 of relaxed columns from the preconditioner's output pass
     blas::Reducer red;
     SolveStats last;
     long long applies = 0;
