@@ -33,41 +33,10 @@
 #include "fdm.h"
 #include "prop.h"
 #include "tsurff.h"
+#include "tsurff_nodes.h"
 
 namespace tdz {
 
-namespace {
-
-// Energy nodes in p = |k + A(T)| (src/tsurff.cpp:700-723): spacing dp_in
-// from p_min up to split = min(max(2 k_cap, p_min), p_max), below which the
-// absorber reflects and the box's quasi-modes set the scale, then dp_out up
-// to p_max; halved until there are four nodes (the cubic weights need them).
-std::vector<double> energy_nodes(double pmin, double pmax, double split, double dp_in, double dp_out) {
-    std::vector<double> node;
-    if (!(pmax > pmin)) return {pmin};
-    // a segment ends exactly at b: a last node a + (b - a) cnt / cnt one
-    // rounding below b would open a second segment of one node next to it,
-    // whose Lagrange weights divide by the rounding difference
-    auto segment = [&](double a, double b, double dp) {
-        if (!(b > a)) return;
-        const int cnt = std::max(1, (int)std::ceil((b - a) / dp - 1e-9));
-        for (int i = node.empty() ? 0 : 1; i <= cnt; ++i) node.push_back(i == cnt ? b : a + (b - a) * i / cnt);
-    };
-    segment(pmin, split, dp_in);
-    segment(node.empty() ? pmin : node.back(), pmax, dp_out);
-    while (node.size() < 4) {
-        std::vector<double> finer;
-        for (size_t i = 0; i + 1 < node.size(); ++i) {
-            finer.push_back(node[i]);
-            finer.push_back(0.5 * (node[i] + node[i + 1]));
-        }
-        finer.push_back(node.back());
-        node.swap(finer);
-    }
-    return node;
-}
-
-}  // namespace
 
 EndTermStats TSurff::end_term(Operator &op, const SolverOptions &so_in, const EndTermOptions &eo, const double2 *psi,
                               std::vector<cd> &out, cudaStream_t st) {
@@ -123,17 +92,10 @@ EndTermStats TSurff::end_term(Operator &op, const SolverOptions &so_in, const En
     // momentum -> four-point Lagrange weights in p on the nodes around p_q,
     // regrouped by node (CSR); one node: weight 1
     std::vector<std::vector<std::pair<int, double>>> per(nn);
-    const int m = std::min(nn, 4);
     for (size_t q = 0; q < nktot; ++q) {
-        if (nn == 1) { per[0].push_back({(int)q, 1.0}); continue; }
-        const int below = (int)(std::upper_bound(node.begin(), node.end(), pk[q]) - node.begin()) - 1;
-        const int j0 = std::max(0, std::min(nn - m, below - 1));
-        for (int a = 0; a < m; ++a) {
-            double w = 1.0;
-            for (int b = 0; b < m; ++b)
-                if (b != a) w *= (pk[q] - node[j0 + b]) / (node[j0 + a] - node[j0 + b]);
-            per[j0 + a].push_back({(int)q, w});
-        }
+        double w[4];
+        const int j0 = lagrange_weights(node, pk[q], w);
+        for (int a = 0; a < std::min(nn, 4); ++a) per[j0 + a].push_back({(int)q, w[a]});
     }
     std::vector<int> start(nn + 1, 0), hq;
     std::vector<double> hw;
