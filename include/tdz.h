@@ -478,6 +478,12 @@ tdz_status tdz_tsurff_end_term(tdz_tsurff *ts, tdz_op *op, const tdz_solver_opts
                                void *stream);
 /* Volkov integrals at the last sample: A[3], B[3], C, t (8 doubles). */
 tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct);
+/* What the spectra file records about the sampler (the attributes of
+ * src/tsurff.cpp:1044-1053), 8 doubles: last sample time, radius, exterior
+ * mass, exterior potential, number of surface points (Gauss nodes on the
+ * 2 dim faces |x_a| = R, src/tsurff.cpp:152-179), number of samples, number
+ * of momenta, dimension. */
+tdz_status tdz_tsurff_info(const tdz_tsurff *ts, double *info);
 void tdz_tsurff_destroy(tdz_tsurff *ts);
 
 /* ------------------------------------------------------ learned correction
@@ -503,6 +509,53 @@ tdz_status tdz_cnn_get_params(const tdz_cnn *n, float *host);
 tdz_status tdz_cnn_set_params(tdz_cnn *n, const float *host);
 tdz_status tdz_cnn_get_grads(const tdz_cnn *n, float *host);
 void tdz_cnn_destroy(tdz_cnn *n);
+
+/* --------------------------------------------------------- output files
+ * HDF5 files of the reference's output schema, written by the library
+ * itself (host only, no HDF5 library): the classic layout that every HDF5
+ * reader opens (version-0 superblock, one root group, contiguous float64
+ * datasets, float64 attributes on the root group).
+ *
+ * tdz_h5_write: a flat file, as the t-SURFF spectra writer makes it
+ * (WriteReal / WriteAttribute, src/tsurff.cpp:74-92,1018-1057). Dataset i
+ * is names[i] of rank ranks[i] (1..8), its extents the next ranks[i]
+ * entries of dims (slowest first, each >= 1), its values data[i]
+ * (row-major). Attribute j is attr_names[j], a rank-1 array of attr_lens[j]
+ * values attr_data[j]. The file is written beside `path` and renamed over
+ * it; parent directories are created. */
+tdz_status tdz_h5_write(const char *path, int ndatasets, const char *const *names, const int *ranks,
+                        const long long *dims, const double *const *data, int nattrs, const char *const *attr_names,
+                        const long long *attr_lens, const double *const *attr_data);
+
+/* The observables file of a propagation (td/<name>_observables.h5):
+ * TDSEZManager::WriteHDF5 (src/manager.cpp:51-201). Five float64 datasets,
+ * one row per recorded step: dipoles (1 + 3 dim columns: t, E_a, D_a, A_a),
+ * populations (1 + n_bound: t, P_n), energies (7: t, Kin, Pot, Int, Tot,
+ * InvMass, Norm), currents (11, or 15 in 3D) and autocorrelation (3: t,
+ * Re C, Im C). Rows are buffered on the host; the file is rewritten with
+ * every row so far when flush_rows rows are pending (<= 0: 5000, the
+ * reference's buffer), on tdz_obsfile_flush and on tdz_obsfile_close, the
+ * first write replacing any file at `path`. The reference appends to
+ * chunked, extendable datasets instead; readers see the same arrays. */
+typedef struct tdz_obsfile tdz_obsfile;
+#define TDZ_OBS_DIPOLES 0
+#define TDZ_OBS_POPULATIONS 1
+#define TDZ_OBS_ENERGIES 2
+#define TDZ_OBS_CURRENTS 3
+#define TDZ_OBS_AUTOCORRELATION 4
+tdz_status tdz_obsfile_open(const char *path, int dim, int n_bound, long long flush_rows, tdz_obsfile **out);
+/* Columns of dataset `set` (TDZ_OBS_*), time column included; -1 for an
+ * unknown set. */
+int tdz_obsfile_columns(const tdz_obsfile *f, int set);
+/* Appends one row at time t to every dataset: rows[set] holds the
+ * columns(set) - 1 values after the time column, or is NULL (zeros); rows
+ * may be NULL. */
+tdz_status tdz_obsfile_record(tdz_obsfile *f, double t, const double *const *rows);
+/* Rows recorded, and rows already in the file. */
+tdz_status tdz_obsfile_rows(const tdz_obsfile *f, long long *recorded, long long *written);
+tdz_status tdz_obsfile_flush(tdz_obsfile *f);
+/* Flushes and frees the handle (freed also when the flush fails). */
+tdz_status tdz_obsfile_close(tdz_obsfile *f);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@ LIB_PATH = _HERE / "libtdz.so"
 TDZ_OK = 0
 TDZ_FP32, TDZ_FP64, TDZ_FP64_DF, TDZ_FP64_F32 = 0, 1, 2, 3
 TDZ_MASS, TDZ_HAMILTONIAN, TDZ_DIPOLE_X, TDZ_DIPOLE_Y, TDZ_DIPOLE_Z, TDZ_STAGE = range(6)
+TDZ_OBS_DIPOLES, TDZ_OBS_POPULATIONS, TDZ_OBS_ENERGIES, TDZ_OBS_CURRENTS, TDZ_OBS_AUTOCORRELATION = range(5)
 
 STATUS_NAMES = {0: "TDZ_OK", 1: "TDZ_ERR_ARG", 2: "TDZ_ERR_CUDA", 3: "TDZ_ERR_NOT_CONVERGED",
                 4: "TDZ_ERR_STATE", 5: "TDZ_ERR_UNSUPPORTED", 6: "TDZ_ERR_BREAKDOWN", 7: "TDZ_ERR_INTERNAL"}
@@ -159,6 +160,15 @@ SIGNATURES = {
     "tdz_cnn_set_params": (I, [VP, C.POINTER(C.c_float)]),
     "tdz_cnn_get_grads": (I, [VP, C.POINTER(C.c_float)]),
     "tdz_cnn_destroy": (None, [VP]),
+    "tdz_tsurff_info": (I, [VP, C.POINTER(D)]),
+    "tdz_h5_write": (I, [C.c_char_p, I, C.POINTER(C.c_char_p), C.POINTER(I), C.POINTER(LL),
+                         C.POINTER(C.POINTER(D)), I, C.POINTER(C.c_char_p), C.POINTER(LL), C.POINTER(C.POINTER(D))]),
+    "tdz_obsfile_open": (I, [C.c_char_p, I, I, LL, PP]),
+    "tdz_obsfile_columns": (I, [VP, I]),
+    "tdz_obsfile_record": (I, [VP, D, C.POINTER(C.POINTER(D))]),
+    "tdz_obsfile_rows": (I, [VP, C.POINTER(LL), C.POINTER(LL)]),
+    "tdz_obsfile_flush": (I, [VP]),
+    "tdz_obsfile_close": (I, [VP]),
 }
 
 

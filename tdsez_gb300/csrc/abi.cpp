@@ -16,6 +16,7 @@
 #include "tgemm.h"
 #include "tsurff.h"
 #include "cnn.h"
+#include "h5file.h"
 
 struct tdz_space {
     tdz::Space s;
@@ -35,6 +36,9 @@ struct tdz_tsurff {
 };
 struct tdz_cnn {
     tdz::CNN n;
+};
+struct tdz_obsfile {
+    tdz::ObsFile f;
 };
 
 namespace tdz {
@@ -652,6 +656,28 @@ tdz_status tdz_tsurff_volkov(const tdz_tsurff *ts, double *abct) {
     });
 }
 
+tdz_status tdz_tsurff_info(const tdz_tsurff *ts, double *info) {
+    return guarded([&] {
+        TDZ_CHECK(ts != nullptr && info != nullptr, TDZ_ERR_ARG, "null argument");
+        const tdz::TSurff &t = ts->t;
+        double points = 0.0;
+        for (int a = 0; a < t.dim; ++a) {
+            double face = 1.0;
+            for (int b = 0; b < 3; ++b)
+                if (b != a && b < t.dim) face *= (double)t.nodes[b].size();
+            points += 2.0 * face;
+        }
+        info[0] = t.prevT;
+        info[1] = t.R;
+        info[2] = t.mass;
+        info[3] = t.V0;
+        info[4] = points;
+        info[5] = (double)t.samples;
+        info[6] = (double)t.nktot;
+        info[7] = (double)t.dim;
+    });
+}
+
 void tdz_tsurff_destroy(tdz_tsurff *ts) { delete ts; }
 
 tdz_status tdz_cnn_create(int cin, int width, int cout, int layers, int D, int H, int W, int batch,
@@ -726,5 +752,76 @@ tdz_status tdz_cnn_get_grads(const tdz_cnn *n, float *host) {
 }
 
 void tdz_cnn_destroy(tdz_cnn *n) { delete n; }
+
+tdz_status tdz_h5_write(const char *path, int ndatasets, const char *const *names, const int *ranks,
+                        const long long *dims, const double *const *data, int nattrs, const char *const *attr_names,
+                        const long long *attr_lens, const double *const *attr_data) {
+    return guarded([&] {
+        TDZ_CHECK(path != nullptr && ndatasets >= 0 && nattrs >= 0, TDZ_ERR_ARG, "invalid arguments");
+        TDZ_CHECK(ndatasets == 0 || (names && ranks && dims && data), TDZ_ERR_ARG, "dataset arrays missing");
+        TDZ_CHECK(nattrs == 0 || (attr_names && attr_lens && attr_data), TDZ_ERR_ARG, "attribute arrays missing");
+        std::vector<tdz::H5Array> ds(ndatasets), at(nattrs);
+        const long long *d = dims;
+        for (int i = 0; i < ndatasets; ++i) {
+            TDZ_CHECK(names[i] != nullptr && ranks[i] >= 1 && ranks[i] <= 8, TDZ_ERR_ARG, "dataset name or rank");
+            ds[i].name = names[i];
+            for (int k = 0; k < ranks[i]; ++k) {
+                TDZ_CHECK(d[k] >= 1, TDZ_ERR_ARG, std::string("dataset '") + names[i] + "' has an empty axis");
+                ds[i].dims.push_back((uint64_t)d[k]);
+            }
+            d += ranks[i];
+            ds[i].data = data[i];
+        }
+        for (int j = 0; j < nattrs; ++j) {
+            TDZ_CHECK(attr_names[j] != nullptr && attr_lens[j] >= 1, TDZ_ERR_ARG, "attribute name or length");
+            at[j].name = attr_names[j];
+            at[j].dims = {(uint64_t)attr_lens[j]};
+            at[j].data = attr_data[j];
+        }
+        tdz::h5_write_file(path, ds, at);
+    });
+}
+
+tdz_status tdz_obsfile_open(const char *path, int dim, int n_bound, long long flush_rows, tdz_obsfile **out) {
+    return guarded([&] {
+        TDZ_CHECK(path != nullptr && out != nullptr, TDZ_ERR_ARG, "null argument");
+        *out = new tdz_obsfile{tdz::ObsFile(path, dim, n_bound, flush_rows)};
+    });
+}
+
+int tdz_obsfile_columns(const tdz_obsfile *f, int set) {
+    if (!f || set < 0 || set >= tdz::ObsFile::kSets) return -1;
+    return f->f.columns(set);
+}
+
+tdz_status tdz_obsfile_record(tdz_obsfile *f, double t, const double *const *rows) {
+    return guarded([&] {
+        TDZ_CHECK(f != nullptr, TDZ_ERR_ARG, "null file");
+        f->f.record(t, rows);
+    });
+}
+
+tdz_status tdz_obsfile_rows(const tdz_obsfile *f, long long *recorded, long long *written) {
+    return guarded([&] {
+        TDZ_CHECK(f != nullptr, TDZ_ERR_ARG, "null file");
+        if (recorded) *recorded = f->f.rows();
+        if (written) *written = f->f.written();
+    });
+}
+
+tdz_status tdz_obsfile_flush(tdz_obsfile *f) {
+    return guarded([&] {
+        TDZ_CHECK(f != nullptr, TDZ_ERR_ARG, "null file");
+        f->f.flush();
+    });
+}
+
+tdz_status tdz_obsfile_close(tdz_obsfile *f) {
+    const tdz_status st = guarded([&] {
+        if (f) f->f.flush();
+    });
+    delete f;
+    return st;
+}
 
 }  // extern "C"

@@ -26,6 +26,7 @@ class TSurff:
             o.kmin[d], o.kmax[d], o.nk[d] = kgrid[d][0], kgrid[d][1], int(kgrid[d][2])
         o.mass, o.v0, o.charge, o.dt = mass, v0, charge, dt
         self.nk = [int(kgrid[d][2]) for d in range(space.dim)]
+        self.kgrid = [(float(kgrid[d][0]), float(kgrid[d][1]), int(kgrid[d][2])) for d in range(space.dim)]
 
         def cb(axis, t, ctx):
             try:
@@ -37,6 +38,12 @@ class TSurff:
         h = C.c_void_p()
         _lib.check(_lib.load().tdz_tsurff_create(space.handle, C.byref(o), self._cb, None, C.byref(h)))
         self.handle = h
+
+    def k_axes(self):
+        """Momentum axes of the grid, the values the sampler uses:
+        k_i = kmin + i (kmax - kmin) / (nk - 1)."""
+        return [np.array([lo if n == 1 else lo + i * (hi - lo) / (n - 1) for i in range(n)])
+                for lo, hi, n in self.kgrid]
 
     def sample(self, t: float, psi, stream=None):
         import torch
