@@ -13,6 +13,8 @@ libtdz itself (no HDF5 library is linked; any HDF5 reader opens them):
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
+import math
 from typing import Callable, Mapping, Optional, Sequence
 
 import numpy as np
@@ -118,9 +120,12 @@ class ObservablesMonitor:
 
     * dipoles: t, E_a(t), D_a = q Re<psi|D_a|psi>; the acceleration A_a is
       not computed (zeros);
-    * energies: t, Kin and Pot not split (zeros), Int = s E(t).<psi|r|psi>,
-      Tot = Re<psi|H|psi> + Int, InvMass (zero), Norm = <psi|M|psi>
-      (unnormalised expectation values, s = -q);
+    * energies: t, Kin = <psi|K|psi>, Pot = Re<psi|H|psi> - Kin (= <sV>:
+      the absorbing potential -iW adds only to the imaginary part),
+      Int = s E(t).<psi|r|psi>, Tot = Re<psi|H|psi> + Int, InvMass =
+      <psi|1/m|psi>, Norm = <psi|M|psi> (unnormalised expectation values,
+      s = -q); K and 1/m are applied by two more operator sets of the same
+      space (the kinetic term alone; 1/m as a potential);
     * populations: t, |<phi_n|M|psi>|^2 for the given bound states;
     * autocorrelation: t, <psi(0)|M|psi(t)> with psi(0) the state at the
       first call;
@@ -138,6 +143,17 @@ class ObservablesMonitor:
         self.file = ObservablesFile(path, self.dim, len(self.bound), flush_rows)
         self._mv = None          # M phi_n ..., M psi(0) (device vectors)
         self._out = None
+        from .operators import Operator, Physics
+        ph = op.phys
+        # the kinetic term alone: the same carrier without potential, soft-core centres and CAP
+        self.op_kin = Operator(op.space, dataclasses.replace(ph, potential=(), cap_kmin=None, softcore=()))
+        self.op_inv = None
+        self.inv_mass = 1.0 / ph.mass
+        if ph.mass_axis is not None:
+            # <1/m> as the expectation value of a potential V = 1/m(x_a) with no kinetic term (s = +1)
+            pot = [ph.inv_mass_fn if d == ph.mass_axis else None for d in range(self.dim)]
+            self.op_inv = Operator(op.space, Physics(charge=-1.0, mass=math.inf, potential=pot, coupled=(),
+                                                     dirichlet=ph.dirichlet))
 
     def _prepare(self, psi):
         import torch
@@ -156,6 +172,8 @@ class ObservablesMonitor:
             self._prepare(psi)
         s = torch.cuda.current_stream().cuda_stream
         norm, energy, dip = self.op.observables(psi)
+        kin = self.op_kin.observables(psi)[1].real
+        inv = self.op_inv.observables(psi)[1].real if self.op_inv is not None else self.inv_mass * norm
         k = len(self._mv)
         _lib.check(_lib.load().tdz_vec_mdot(self._ptrs, k, C.c_void_p(psi.data_ptr()), psi.numel(), _lib.TDZ_FP64,
                                             C.c_void_p(self._out.data_ptr()), C.c_void_p(s)))
@@ -171,7 +189,7 @@ class ObservablesMonitor:
             t,
             dipoles=np.concatenate([e[:self.dim], self.q * x, np.zeros(self.dim)]),
             populations=np.abs(proj[:-1]) ** 2,
-            energies=[0.0, 0.0, e_int, energy.real + e_int, 0.0, norm],
+            energies=[kin, energy.real - kin, e_int, energy.real + e_int, inv, norm],
             autocorrelation=[proj[-1].real, proj[-1].imag])
 
     def close(self) -> None:

@@ -1,5 +1,7 @@
 """Output files from GPU runs, read back with tests/h5lite.py: the
-observables monitor's rows against the oracle's assembled matrices (1e-12),
+observables monitor's rows (dipoles, the energy split, <1/m>, populations,
+autocorrelation) against the oracle's assembled matrices (1e-12), on a 2D
+case with a CAP and a 1D case with a layered mass,
 and the t-SURFF spectra file against the sampler's own amplitudes and the
 reference's schema (src/tsurff.cpp:1018-1057)."""
 import math
@@ -13,20 +15,27 @@ from tests.cases import CASES, oracle_of, product_of
 
 
 @pytest.mark.gpu
-def test_observables_monitor_rows(cuda, tmp_path):
+@pytest.mark.parametrize("name", ["2d_cap_softcore_sep", "1d_layered_mass"])
+def test_observables_monitor_rows(cuda, tmp_path, name):
+    import scipy.sparse as sp
     import torch
+    from oracle import operators as oo
     from tdsez_gb300.outputs import ObservablesMonitor
     from tdsez_gb300.propagator import Propagator
-    c = CASES["2d_cap_softcore_sep"]()
+    c = CASES[name]()
     S, ph, A = oracle_of(c)
     PS, op = product_of(c)
+    dim = S.dim
     rng = np.random.default_rng(3)
     psi0 = rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof)
     psi0 /= math.sqrt(np.vdot(psi0, A.M @ psi0).real)
     phi = [rng.standard_normal(S.ndof) + 1j * rng.standard_normal(S.ndof) for _ in range(2)]
+    coords = [cc.reshape(-1) for cc in S.quad_coords()]
+    w = S.quad_weights().reshape(-1)
+    Minv = (A.B.T @ sp.diags(w * oo._eval_grid(ph.minv, coords, dim)) @ A.B).tocsr()
 
     def field(t):
-        return [0.02 * math.sin(0.5 * t), 0.0]
+        return [0.02 * math.sin(0.5 * t), 0.0][:dim]
     q = c["charge"]
     mon = ObservablesMonitor(tmp_path / "td" / "run_observables.h5", op, field=field, charge=q,
                              bound=[torch.tensor(v, device=cuda) for v in phi], flush_rows=3)
@@ -42,26 +51,33 @@ def test_observables_monitor_rows(cuda, tmp_path):
     f = h5lite.File(str(tmp_path / "td" / "run_observables.h5"))
     dip, ene, pop, auto, cur = (f[s].read() for s in ("dipoles", "energies", "populations", "autocorrelation",
                                                      "currents"))
-    assert dip.shape == (6, 7) and ene.shape == (6, 7) and pop.shape == (6, 3) and cur.shape == (6, 11)
+    assert dip.shape == (6, 1 + 3 * dim) and ene.shape == (6, 7) and pop.shape == (6, 3) and cur.shape == (6, 11)
     H = A.H_total()
     for r, (t, x) in enumerate(states):
         n = np.vdot(x, A.M @ x).real
         e = np.vdot(x, H @ x)
-        d = [np.vdot(x, A.D[a] @ x).real for a in range(2)]
+        kin = np.vdot(x, A.K @ x).real
+        pot = np.vdot(x, A.V @ x).real
+        inv = np.vdot(x, Minv @ x).real
+        d = [np.vdot(x, A.D[a] @ x).real for a in range(dim)]
         E = field(t)
-        e_int = -q * (E[0] * d[0] + E[1] * d[1])
+        e_int = -q * sum(E[a] * d[a] for a in range(dim))
         assert all(row[0] == t for row in (dip[r], ene[r], pop[r], auto[r], cur[r]))
-        assert np.array_equal(dip[r, 1:3], E) and np.array_equal(dip[r, 5:], [0.0, 0.0])
-        assert np.allclose(dip[r, 3:5], [q * d[0], q * d[1]], rtol=1e-12, atol=1e-12 * n)
-        assert abs(ene[r, 6] - n) <= 1e-12 * n
+        assert np.array_equal(dip[r, 1:1 + dim], E) and not np.any(dip[r, 1 + 2 * dim:])
+        assert np.allclose(dip[r, 1 + dim:1 + 2 * dim], [q * v for v in d], rtol=1e-12, atol=1e-12 * n)
+        scale = abs(e) + abs(kin) + n
+        assert abs(ene[r, 1] - kin) <= 1e-12 * scale
+        assert abs(ene[r, 2] - pot) <= 1e-12 * scale
         assert abs(ene[r, 3] - e_int) <= 1e-12 * (abs(e_int) + n)
-        assert abs(ene[r, 4] - (e.real + e_int)) <= 1e-12 * (abs(e) + n)
+        assert abs(ene[r, 4] - (e.real + e_int)) <= 1e-12 * scale
+        assert abs(ene[r, 5] - inv) <= 1e-12 * inv
+        assert abs(ene[r, 6] - n) <= 1e-12 * n
         for i, v in enumerate(phi):
             ref = abs(np.vdot(v, A.M @ x)) ** 2
             assert abs(pop[r, 1 + i] - ref) <= 1e-11 * ref
         ac = np.vdot(psi0, A.M @ x)
         assert abs(auto[r, 1] + 1j * auto[r, 2] - ac) <= 1e-12
-        assert not np.any(cur[r, 1:]) and not np.any(ene[r, [1, 2, 5]])
+        assert not np.any(cur[r, 1:])
     assert abs(auto[0, 1] - 1.0) < 1e-12 and abs(auto[0, 2]) < 1e-12
 
 
