@@ -536,7 +536,9 @@ tdz_status tdz_h5_write(const char *path, int ndatasets, const char *const *name
  * every row so far when flush_rows rows are pending (<= 0: 5000, the
  * reference's buffer), on tdz_obsfile_flush and on tdz_obsfile_close, the
  * first write replacing any file at `path`. The reference appends to
- * chunked, extendable datasets instead; readers see the same arrays. */
+ * chunked, extendable datasets instead; readers see the same arrays. A
+ * handle is used by one thread at a time (the reference writes from rank 0
+ * only); different handles are independent. */
 typedef struct tdz_obsfile tdz_obsfile;
 #define TDZ_OBS_DIPOLES 0
 #define TDZ_OBS_POPULATIONS 1
