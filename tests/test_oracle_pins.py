@@ -142,3 +142,41 @@ def test_tsurff_free_packet():
     ex = (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ks - k0) ** 2)
     tot = amp + ts.interior(psi, [ks])
     assert np.abs(np.abs(tot) ** 2 - ex).max() / ex.max() < 1e-4
+
+
+@pytest.mark.parametrize("charge", [-1.0, 1.0])
+def test_tsurff_field_mass_offset(charge):
+    """Canonical momentum is conserved (test_tsurff.py:93-103): the FREE1D
+    packet under the pulse 0.2 sin^2(pi t/15) sin(1.3 t) (t < 15), with mass
+    0.5, a constant potential 0.3 (exterior potential s V = -q 0.3) and
+    either carrier sign, stopped at T = 15: flux plus interior term give the
+    field-free analytic spectrum to 2e-4 of its peak, and A(T) != 0."""
+    import scipy.sparse.linalg as sla
+    p, L = 7, 40.0
+    ax = ob.Axis(ob.uniform_knots(400, -L, L, p), p, 10)
+    S = ob.Space([ax])
+    A = oo.Assembled(S, oo.Physics(dim=1, charge=charge, potential=lambda x, y, z: 0.3, mass_const=0.5,
+                                   cap_kmin=0.5, bounds=[(-L, L)]))
+
+    def field(t):
+        return [0.2 * math.sin(math.pi * t / 15) ** 2 * math.sin(1.3 * t) if t < 15 else 0.0]
+    w, k0 = 1.0, 2.0
+    g = (2 * np.pi * w * w) ** -0.25 * np.exp(-ax.xq.reshape(-1) ** 2 / (4 * w * w) + 1j * k0 * ax.xq.reshape(-1))
+    psi = sla.spsolve(A.M.tocsc().astype(complex), ax.basis_matrix(0).T @ (ax.wq.reshape(-1) * g))
+    dt, T = 0.025, 15.0
+    ks = np.linspace(-1.0, 5.0, 61)
+    s = -charge
+    ts = ots.OracleTSurff(S, 10.0, [ks], 0.5, s * 0.3, s, lambda t: [field(t)[0], 0.0, 0.0], dt)
+    amp = ts.add_flux(0.0, psi, [ks], np.zeros(len(ks), dtype=complex))
+
+    def observe(t, x):
+        nonlocal amp
+        if t > 0:
+            amp = ts.add_flux(t, x, [ks], amp)
+    psi, _ = op.OraclePropagator(A, field, "pade22").evolve(psi, dt, T, observe=observe)
+    tot = amp + ts.interior(psi, [ks])
+    ex = (2 * w * w / np.pi) ** 0.5 * np.exp(-2 * w * w * (ks - k0) ** 2)
+    err = np.abs(np.abs(tot) ** 2 - ex).max() / ex.max()
+    print("charge", charge, "spectrum error", err, "A(T)", ts.A[0])
+    assert err < 2e-4, err
+    assert abs(ts.A[0]) > 1e-3
