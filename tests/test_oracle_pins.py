@@ -180,3 +180,32 @@ def test_tsurff_field_mass_offset(charge):
     print("charge", charge, "spectrum error", err, "A(T)", ts.A[0])
     assert err < 2e-4, err
     assert abs(ts.A[0]) > 1e-3
+
+
+def test_quesne_position_dependent_mass():
+    """Quesne oscillator (test_analytic.py:136-157): m(x) = (1 + x/2)^-1,
+    V = x^2 / (4 (x + 2)) on [-1.999999999, 50] with Dirichlet walls, p = 7,
+    1000 elements, 10 Gauss points: E_n = (n + 1/2) / 2 to 1e-9."""
+    ax = ob.Axis(ob.uniform_knots(1000, -1.999999999, 50.0, 7), 7, 10)
+    A = oo.Assembled(ob.Space([ax]), oo.Physics(dim=1, potential=lambda x, y, z: x * x / (4.0 * (x + 2.0)),
+                                                inv_mass=lambda x, y, z: 1.0 + x / 2.0, mass_const=None,
+                                                mass_axis=0, dirichlet=True))
+    E = _eig(A, 5)
+    assert np.abs(E - 0.5 * (np.arange(5) + 0.5)).max() < 1e-9, E
+
+
+def test_hole_inverts_potential_and_coupling():
+    """Charge +1 (test_analytic.py:276-296): H = K - (V + x E) with
+    V = -x^2/2 is the oscillator for the hole (E = 1/2, 3/2, 5/2), and the
+    drive 0.5 cos(0.6 t) pushes it the other way: the dipole q<x> = +<x>
+    follows +0.5/(1 - 0.36) (cos 0.6t - cos t) to 1e-4 (Magnus-4, dt 0.05,
+    T = 20)."""
+    ax = ob.Axis(ob.uniform_knots(120, -20.0, 20.0, 7), 7, 10)
+    A = oo.Assembled(ob.Space([ax]), oo.Physics(dim=1, charge=1.0, potential=lambda x, y, z: -0.5 * x * x))
+    assert np.abs(_eig(A, 3) - [0.5, 1.5, 2.5]).max() < 1e-8
+    _, V = op.ground_state(A, 0.5)
+    P = op.OraclePropagator(A, lambda t: [0.5 * np.cos(0.6 * t)], "magnus4")
+    _, out = P.evolve(V[:, 0], 0.05, 20.0, lambda t, psi: (t, op.expect(A.D[0], psi).real))
+    out = np.array(out)
+    x = 0.5 / (1 - 0.36) * (np.cos(0.6 * out[:, 0]) - np.cos(out[:, 0]))
+    assert np.abs(1.0 * out[:, 1] - x).max() < 1e-4
