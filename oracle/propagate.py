@@ -46,6 +46,19 @@ class OraclePropagator:
         self.H = asm.H_total().astype(np.complex128).tocsc()
         self.T = [D.astype(np.complex128).tocsc() for D in asm.terms()]
         self.s = asm.phys.sign
+        self._lu = {}     # (scale, coefficients) -> LU of M + scale H_E, for repeated stages
+
+    def _solve(self, scale, c, rhs):
+        """(M + scale H_E(c))^-1 rhs by a sparse LU, kept while the stage
+        repeats (a field that is off, or constant)."""
+        key = (complex(scale), tuple(complex(v) for v in c))
+        lu = self._lu.get(key)
+        if lu is None:
+            if len(self._lu) >= 4:
+                self._lu.clear()
+            lu = sla.splu((self.M + scale * self.H_E(c)).tocsc())
+            self._lu[key] = lu
+        return lu.solve(rhs)
 
     def coeffs(self, t: float):
         return [self.s * e for e in self.field(t)]
@@ -58,9 +71,7 @@ class OraclePropagator:
         return A
 
     def cn_step(self, psi, t, h):
-        HE = self.H_E(self.coeffs(t + 0.5 * h))
-        A = (self.M + 0.5j * h * HE).tocsc()
-        X = sla.spsolve(A, self.M @ psi)
+        X = self._solve(0.5j * h, self.coeffs(t + 0.5 * h), self.M @ psi)
         return 2.0 * X - psi
 
     def pade_step(self, psi, h, c):
@@ -69,7 +80,7 @@ class OraclePropagator:
         x = psi
         for k in range(2):
             rhs = 2.0 * (self.M @ x) - A[1 - k] @ x
-            x = sla.spsolve(A[k], rhs)
+            x = self._solve(PADE_G[k] * h, c, rhs)
         return x
 
     def step(self, psi, t, h):

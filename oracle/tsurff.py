@@ -135,18 +135,20 @@ class OracleTSurff:
         dn = self.Tn @ psi
         ks = [np.asarray(kgrid[d]) if d < self.dim else np.array([0.0]) for d in range(3)]
         K = np.stack(np.meshgrid(*ks, indexing="ij"), axis=-1).reshape(-1, 3)
-        out = np.zeros(len(K), dtype=np.complex128)
         norm = (2 * math.pi) ** (-0.5 * self.dim)
-        for i, k in enumerate(K):
-            phi = self.C + np.sum(self.vt * k * k / (2 * self.mass) + k * self.B / self.mass)
+        X = np.array([pt[0] for pt in self.points])                  # surface points (P, 3)
+        W = np.array([pt[1] for pt in self.points])
+        axis = np.array([pt[2] // 2 for pt in self.points])
+        sigma = np.array([1.0 if pt[2] % 2 else -1.0 for pt in self.points])
+        im = np.array([pt[3] for pt in self.points])
+        out = np.zeros(len(K), dtype=np.complex128)
+        for i0 in range(0, len(K), 256):            # blocks of momenta: every point at once
+            k = K[i0:i0 + 256]
+            phi = self.C + np.sum(self.vt * k * k / (2 * self.mass) + k * self.B / self.mass, axis=1)
             kA = k + self.A
-            tot = 0j
-            for q, (x, w, face, im) in enumerate(self.points):
-                a = face // 2
-                sigma = 1.0 if face % 2 else -1.0
-                chi = w * np.exp(1j * (phi - kA @ x))
-                tot += chi * (-dn[q] - 1j * sigma * im * kA[a] * v[q])
-            out[i] = 0.5j * norm * tot
+            chi = W * np.exp(1j * (phi[:, None] - kA @ X.T))
+            term = -dn[None, :] - 1j * (sigma * im)[None, :] * kA[:, axis] * v[None, :]
+            out[i0:i0 + 256] = 0.5j * norm * np.sum(chi * term, axis=1)
         return out
 
     def add_flux(self, t, psi, kgrid, amp):

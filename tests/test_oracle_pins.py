@@ -209,3 +209,41 @@ def test_hole_inverts_potential_and_coupling():
     out = np.array(out)
     x = 0.5 / (1 - 0.36) * (np.cos(0.6 * out[:, 0]) - np.cos(out[:, 0]))
     assert np.abs(1.0 * out[:, 1] - x).max() < 1e-4
+
+
+def test_tsurff_free_packet_2d():
+    """2D deck of test_tsurff.py:122-153: packet with momentum (2, 1) and
+    widths 1 on [-20, 20]^2, 60 elements of degree 4 per axis, CN dt 0.02 to
+    T = 2, CAP k_min 1, R = 6, 31 x 31 momenta on [-1, 5] x [-2, 4]: flux
+    plus interior term against the analytic spectrum, 5e-3 of its peak."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    p, L = 4, 20.0
+    axes = [ob.Axis(ob.uniform_knots(60, -L, L, p), p, 6) for _ in range(2)]
+    S = ob.Space(axes)
+    A = oo.Assembled(S, oo.Physics(dim=2, potential=None, cap_kmin=1.0, bounds=[(-L, L)] * 2, coupled=(0, 1)))
+    w, k0 = 1.0, (2.0, 1.0)
+    part = []
+    for d, ax in enumerate(axes):
+        x = ax.xq.reshape(-1)
+        g = (2 * np.pi * w * w) ** -0.25 * np.exp(-x * x / (4 * w * w) + 1j * k0[d] * x)
+        B = ax.basis_matrix(0)
+        Md = (B.T @ sp.diags(ax.wq.reshape(-1)) @ B).tocsc()
+        part.append(sla.spsolve(Md.astype(complex), ax.basis_matrix(0).T @ (ax.wq.reshape(-1) * g)))
+    psi = np.kron(part[1], part[0])          # x fastest
+    ks = [np.linspace(-1.0, 5.0, 31), np.linspace(-2.0, 4.0, 31)]
+    dt, T = 0.02, 2.0
+    ts = ots.OracleTSurff(S, 6.0, ks, 1.0, 0.0, 1.0, lambda t: [0.0, 0.0, 0.0], dt)
+    amp = ts.add_flux(0.0, psi, ks, np.zeros(31 * 31, dtype=complex))
+
+    def observe(t, x):
+        nonlocal amp
+        if t > 0:
+            amp = ts.add_flux(t, x, ks, amp)
+    psi, _ = op.OraclePropagator(A, lambda t: [0.0, 0.0], "cn").evolve(psi, dt, T, observe=observe)
+    tot = amp + ts.interior(psi, ks)
+    kx, ky = np.meshgrid(ks[0], ks[1], indexing="ij")
+    ex = ((2 * w * w / np.pi) * np.exp(-2 * w * w * ((kx - k0[0]) ** 2 + (ky - k0[1]) ** 2))).reshape(-1)
+    err = np.abs(np.abs(tot) ** 2 - ex).max() / ex.max()
+    print("2D spectrum error", err)
+    assert err < 5e-3, err
