@@ -19,7 +19,7 @@ struct Precond {
     // z = P^-1 r and ||z||^2 into *norm2 (device), in the pass that writes z,
     // where the preconditioner can (has_apply_norm)
     virtual bool has_apply_norm() const { return false; }
-    virtual void apply_norm(const double2 *r, double2 *z, double *norm2, cudaStream_t st) { apply(r, z, st); }
+    virtual void apply_norm(const double2 *r, double2 *z, double * /*norm2*/, cudaStream_t st) { apply(r, z, st); }
 };
 
 struct PcNone : Precond {
